@@ -1,0 +1,227 @@
+"""Python mirror of the fpa.h C API, bound to libfpa_gb300.so with ctypes.
+
+The names, argument order and result codes follow the reference's public header
+(fpa.h:8-63): `FpaArray` plays the role of `fpa_t` (fpa_init / fpa_clear /
+fpa_copy_array_to_device / fpa_copy_array_to_host), and `fpa_add`, `fpa_mul`, ... take
+(r, a, b, mode) and return an `fpa_result` code.  There is no CPU fallback: importing
+this module fails loudly if the CUDA library has not been built.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libfpa_gb300.so")
+
+# fpa.h:8-10
+fpa_round_truncate, fpa_round_up, fpa_round_down, fpa_round_ties_to_even, fpa_round_ties_away_from_zero = range(5)
+MODES = (fpa_round_truncate, fpa_round_up, fpa_round_down, fpa_round_ties_to_even, fpa_round_ties_away_from_zero)
+# fpa.h:12-17 (+ fpa_device_error)
+fpa_success, fpa_math_error, fpa_invalid_precisions, fpa_invalid_counts, fpa_device_error = range(5)
+# fpa_gb300.h
+OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_SQRT = range(5)
+OPS = {"add": OP_ADD, "sub": OP_SUB, "mul": OP_MUL, "div": OP_DIV, "sqrt": OP_SQRT}
+
+BIAS = 0x3FFFFFF3
+
+
+class fpa_s(ctypes.Structure):
+    """fpa.h:19-26"""
+    _fields_ = [("count", ctypes.c_uint32), ("precision", ctypes.c_uint32),
+                ("gpu_exps", ctypes.c_void_p), ("gpu_limbs", ctypes.c_void_p)]
+
+
+class FpaError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load libfpa_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise FpaError(f"CUDA library missing: {LIB_PATH} (run cubigfloat_gb300.build.build())")
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER(fpa_s)
+    u32, u64, i32, vp = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p
+    sig = {
+        "fpa_init": (i32, [P, u32, u32]),
+        "fpa_clear": (i32, [P]),
+        "fpa_copy_array_to_device": (i32, [P, vp, vp]),
+        "fpa_copy_array_to_host": (i32, [P, vp, vp]),
+        "fpa_set_ui": (i32, [P, vp]),
+        "fpa_set_si": (i32, [P, vp]),
+        "fpa_set_float": (i32, [P, vp]),
+        "fpa_set_double": (i32, [P, vp]),
+        "fpa_set": (i32, [P, P, i32]),
+        "fpa_sgn": (i32, [vp, P]),
+        "fpa_cmp": (i32, [vp, P, P]),
+        "fpa_neg": (i32, [P, P]),
+        "fpa_add": (i32, [P, P, P, i32]),
+        "fpa_sub": (i32, [P, P, P, i32]),
+        "fpa_mul": (i32, [P, P, P, i32]),
+        "fpa_div": (i32, [P, P, P, i32]),
+        "fpa_sqrt": (i32, [P, P, i32]),
+        "fpa_gb300_elementwise": (i32, [i32, u32, u64, i32, vp, vp, vp, vp, vp, vp, vp]),
+        "fpa_op_async": (i32, [i32, P, P, P, i32, vp]),
+        "fpa_copy_array_to_device_async": (i32, [P, vp, vp, vp]),
+        "fpa_copy_array_to_host_async": (i32, [P, vp, vp, vp]),
+        "fpa_gb300_device_errors": (u32, []),
+        "fpa_gb300_num_configs": (i32, []),
+        "fpa_gb300_config_shape": (i32, [i32, ctypes.POINTER(u32), ctypes.POINTER(u32)]),
+        "fpa_gb300_set_config": (i32, [u32, i32]),
+        "fpa_gb300_get_config": (i32, [u32]),
+        "fpa_gb300_version": (ctypes.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class FpaArray:
+    """An fpa_t: `count` numbers of `precision` bits in device memory."""
+
+    def __init__(self, count, precision):
+        self.s = fpa_s()
+        rc = lib().fpa_init(ctypes.byref(self.s), count, precision)
+        if rc != fpa_success:
+            raise FpaError(f"fpa_init({count}, {precision}) -> {rc}")
+        self._live = True
+
+    @property
+    def count(self):
+        return self.s.count
+
+    @property
+    def precision(self):
+        return self.s.precision
+
+    @property
+    def limbs(self):
+        return self.s.precision // 32
+
+    @property
+    def ref(self):
+        return ctypes.byref(self.s)
+
+    def to_device(self, exps, limbs):
+        exps = np.ascontiguousarray(exps, dtype=np.uint32)
+        limbs = np.ascontiguousarray(limbs, dtype=np.uint32)
+        assert exps.size == self.count and limbs.size == self.count * self.limbs
+        return lib().fpa_copy_array_to_device(self.ref, _ptr(exps), _ptr(limbs))
+
+    def to_host(self):
+        exps = np.zeros(self.count, dtype=np.uint32)
+        limbs = np.zeros((self.count, self.limbs), dtype=np.uint32)
+        rc = lib().fpa_copy_array_to_host(self.ref, _ptr(exps), _ptr(limbs))
+        if rc != fpa_success:
+            raise FpaError(f"fpa_copy_array_to_host -> {rc}")
+        return exps, limbs
+
+    def clear(self):
+        if self._live:
+            lib().fpa_clear(self.ref)
+            self._live = False
+
+    def __del__(self):
+        try:
+            self.clear()
+        except Exception:
+            pass
+
+
+def fpa_add(r, a, b, mode):
+    return lib().fpa_add(r.ref, a.ref, b.ref, mode)
+
+
+def fpa_sub(r, a, b, mode):
+    return lib().fpa_sub(r.ref, a.ref, b.ref, mode)
+
+
+def fpa_mul(r, a, b, mode):
+    return lib().fpa_mul(r.ref, a.ref, b.ref, mode)
+
+
+def fpa_div(r, a, b, mode):
+    return lib().fpa_div(r.ref, a.ref, b.ref, mode)
+
+
+def fpa_sqrt(r, x, mode):
+    return lib().fpa_sqrt(r.ref, x.ref, mode)
+
+
+def fpa_neg(r, a):
+    return lib().fpa_neg(r.ref, a.ref)
+
+
+def fpa_set(r, x, mode):
+    return lib().fpa_set(r.ref, x.ref, mode)
+
+
+def fpa_set_ui(r, values):
+    v = np.ascontiguousarray(values, dtype=np.uint64)
+    return lib().fpa_set_ui(r.ref, _ptr(v))
+
+
+def fpa_set_si(r, values):
+    v = np.ascontiguousarray(values, dtype=np.int64)
+    return lib().fpa_set_si(r.ref, _ptr(v))
+
+
+def fpa_set_float(r, values):
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    return lib().fpa_set_float(r.ref, _ptr(v))
+
+
+def fpa_set_double(r, values):
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    return lib().fpa_set_double(r.ref, _ptr(v))
+
+
+def fpa_sgn(r_dev_ptr, x):
+    """r_dev_ptr: device address of `count` int32 results."""
+    return lib().fpa_sgn(ctypes.c_void_p(r_dev_ptr), x.ref)
+
+
+def fpa_cmp(r_dev_ptr, a, b):
+    return lib().fpa_cmp(ctypes.c_void_p(r_dev_ptr), a.ref, b.ref)
+
+
+def elementwise(op, precision, count, mode, r_exps, r_limbs, a_exps, a_limbs, b_exps=0, b_limbs=0, stream=0):
+    """fpa_gb300_elementwise on raw device addresses (ints)."""
+    v = ctypes.c_void_p
+    return lib().fpa_gb300_elementwise(op, precision, count, mode, v(r_exps), v(r_limbs), v(a_exps), v(a_limbs),
+                                       v(b_exps), v(b_limbs), v(stream))
+
+
+def device_errors():
+    return lib().fpa_gb300_device_errors()
+
+
+def configs():
+    out = []
+    for c in range(lib().fpa_gb300_num_configs()):
+        g, k = ctypes.c_uint32(), ctypes.c_uint32()
+        lib().fpa_gb300_config_shape(c, ctypes.byref(g), ctypes.byref(k))
+        out.append((g.value, k.value))
+    return out
+
+
+def set_config(limbs, cfg):
+    return lib().fpa_gb300_set_config(limbs, cfg)
+
+
+def get_config(limbs):
+    return lib().fpa_gb300_get_config(limbs)

@@ -1,0 +1,119 @@
+// fpa_kernels.cu -- elementwise fpa kernels for one lane-group configuration.
+//
+// This file is compiled once per configuration (GFPA_CFG selects G lanes per operation
+// and K limbs per product tile, capacity N = G*K limbs) so the configurations build in
+// parallel.  Each object exports gfpa_launch_cfg<i>() used by the host dispatcher.
+#include <cuda_runtime.h>
+#include "fpa_ops.cuh"
+#include "fpa_launch.h"
+
+#ifndef GFPA_CFG
+#define GFPA_CFG 4
+#endif
+
+#if GFPA_CFG == 0
+#define CFG_G 4
+#define CFG_K 2
+#elif GFPA_CFG == 1
+#define CFG_G 8
+#define CFG_K 2
+#elif GFPA_CFG == 2
+#define CFG_G 8
+#define CFG_K 4
+#elif GFPA_CFG == 3
+#define CFG_G 16
+#define CFG_K 4
+#elif GFPA_CFG == 4
+#define CFG_G 32
+#define CFG_K 4
+#elif GFPA_CFG == 5
+#define CFG_G 32
+#define CFG_K 8
+#elif GFPA_CFG == 6
+#define CFG_G 32
+#define CFG_K 16
+#else
+#error "unknown GFPA_CFG"
+#endif
+
+#define GFPA_CAT2(a, b) a##b
+#define GFPA_CAT(a, b) GFPA_CAT2(a, b)
+#define GFPA_LAUNCH_NAME GFPA_CAT(gfpa_launch_cfg, GFPA_CFG)
+
+namespace gfpa {
+
+template <int OP, int G, int K>
+struct Words {
+  __host__ __device__ static constexpr int v() {
+    return MulScratch<G, K>::words() +
+           (OP == OP_ADD || OP == OP_SUB ? OpSpace<G, K>::addsub()
+            : OP == OP_MUL ? OpSpace<G, K>::mul()
+            : OP == OP_DIV ? OpSpace<G, K>::div() : OpSpace<G, K>::sqrt());
+  }
+  // keep each group's slice 16-byte aligned
+  __host__ __device__ static constexpr int aligned() { return (v() + 3) & ~3; }
+};
+
+template <int OP, int G, int K>
+__global__ void __launch_bounds__(128) k_elementwise(ElementwiseArgs args) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  Grp<G> g;
+  const uint32_t gpc = blockDim.x / G, gi = threadIdx.x / G;
+  uint32_t *ws = smem + gi * Words<OP, G, K>::aligned();
+  const int n = (int)args.n;
+  for (uint64_t i = (uint64_t)blockIdx.x * gpc + gi; i < args.count; i += (uint64_t)gridDim.x * gpc) {
+    const uint64_t off = i * (uint64_t)n;
+    const uint32_t a_exp = args.a_exps[i];
+    const uint32_t b_exp = (OP == OP_SQRT) ? 0u : args.b_exps[i];
+    if (OP == OP_ADD || OP == OP_SUB)
+      op_addsub<G, K>(g, ws, n, args.mode, OP == OP_SUB, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
+                      args.r_exps + i, args.r_limbs + off);
+    else if (OP == OP_MUL)
+      op_mul<G, K>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
+                   args.r_exps + i, args.r_limbs + off);
+    else if (OP == OP_DIV)
+      op_div<G, K>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
+                   args.r_exps + i, args.r_limbs + off, args.err);
+    else
+      op_sqrt<G, K>(g, ws, n, args.mode, a_exp, args.a_limbs + off, args.r_exps + i, args.r_limbs + off, args.err);
+    g.sync();   // the group's shared slice is reused by its next instance
+  }
+}
+
+template <int OP>
+static cudaError_t launch_op(const ElementwiseArgs &args, cudaStream_t stream, int sms) {
+  constexpr int G = CFG_G, K = CFG_K;
+  constexpr int threads = 128;
+  constexpr int gpc = threads / G;
+  const size_t smem = (size_t)gpc * Words<OP, G, K>::aligned() * sizeof(uint32_t);
+  static int configured = 0, per_sm = 1;
+  auto kern = k_elementwise<OP, G, K>;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    configured = 1;
+  }
+  const uint64_t need = (args.count + gpc - 1) / gpc;
+  const uint64_t cap = (uint64_t)sms * (uint64_t)per_sm;
+  const unsigned grid = (unsigned)(need < cap ? need : cap);
+  if (grid == 0) return cudaSuccess;
+  kern<<<grid, threads, smem, stream>>>(args);
+  return cudaGetLastError();
+}
+
+}  // namespace gfpa
+
+extern "C" cudaError_t GFPA_LAUNCH_NAME(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms) {
+  using namespace gfpa;
+  switch (op) {
+    case OP_ADD: return launch_op<OP_ADD>(*args, stream, sms);
+    case OP_SUB: return launch_op<OP_SUB>(*args, stream, sms);
+    case OP_MUL: return launch_op<OP_MUL>(*args, stream, sms);
+    case OP_DIV: return launch_op<OP_DIV>(*args, stream, sms);
+    case OP_SQRT: return launch_op<OP_SQRT>(*args, stream, sms);
+  }
+  return cudaErrorInvalidValue;
+}

@@ -1,0 +1,55 @@
+// fpa_launch.h -- internal host/device interface between the C-ABI layer and the kernels.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+// One elementwise launch: `count` instances of `n` limbs each, contiguous per instance
+// (instance i's limbs at i*n), exponent words in separate arrays.  All pointers are device
+// pointers.  b_* are ignored for sqrt.  `err` is a device word the kernels OR error bits
+// into (1: div correction did not converge, 2: sqrt correction did not converge).
+struct ElementwiseArgs {
+  uint64_t count;
+  uint32_t n;
+  int mode;
+  uint32_t *r_exps, *r_limbs;
+  const uint32_t *a_exps, *a_limbs;
+  const uint32_t *b_exps, *b_limbs;
+  uint32_t *err;
+};
+
+#define GFPA_NUM_CFGS 7
+#define GFPA_MAX_LIMBS 512
+
+// limb capacity of each lane-group configuration (G lanes x K limbs per tile)
+static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32};
+static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16};
+
+extern "C" {
+cudaError_t gfpa_launch_cfg0(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg1(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg2(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg3(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg4(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg5(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg6(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+}
+
+// smallest configuration whose capacity holds n limbs
+static inline int gfpa_default_cfg(uint32_t n) {
+  for (int c = 0; c < GFPA_NUM_CFGS; c++)
+    if ((uint32_t)(gfpa_cfg_G[c] * gfpa_cfg_K[c]) >= n) return c;
+  return -1;
+}
+
+static inline cudaError_t gfpa_launch(int cfg, int op, const ElementwiseArgs *args, cudaStream_t stream, int sms) {
+  switch (cfg) {
+    case 0: return gfpa_launch_cfg0(op, args, stream, sms);
+    case 1: return gfpa_launch_cfg1(op, args, stream, sms);
+    case 2: return gfpa_launch_cfg2(op, args, stream, sms);
+    case 3: return gfpa_launch_cfg3(op, args, stream, sms);
+    case 4: return gfpa_launch_cfg4(op, args, stream, sms);
+    case 5: return gfpa_launch_cfg5(op, args, stream, sms);
+    case 6: return gfpa_launch_cfg6(op, args, stream, sms);
+  }
+  return cudaErrorInvalidValue;
+}

@@ -1,0 +1,402 @@
+// fpa_ops.cuh -- one fpa operation (add/sub/mul/div/sqrt) executed by one lane group.
+//
+// Every operation computes its mantissa result exactly (or exactly enough: an integer
+// part plus an exact sticky flag) and rounds once with grp_round, so the result is the
+// correctly rounded value for the requested mode.  Special operands follow the action
+// tables of fpa_device.cuh; exponent range limits follow the reference kernels cited
+// at each operation.
+#pragma once
+#include "fpa_device.cuh"
+
+namespace gfpa {
+
+// Workspace words per group, beyond MulScratch.  N = G*K is the group's limb capacity.
+template <int G, int K>
+struct OpSpace {
+  static constexpr int N = G * K;
+  __host__ __device__ static constexpr int addsub() { return 3 * N + 8; }
+  __host__ __device__ static constexpr int mul() { return 2 * N + 4; }
+  __host__ __device__ static constexpr int div() { return 2 * N + (N + 4) * 2 + (2 * N + 8) * 2 + (N + 8) * 3; }
+  __host__ __device__ static constexpr int sqrt() { return N + (2 * N + 4) + (N + 4) * 2 + (2 * N + 8) * 5 + (N + 8) * 2; }
+  __host__ __device__ static constexpr int max_all() {
+    int a = addsub(), b = mul(), c = div(), d = sqrt();
+    int m = a > b ? a : b; m = m > c ? m : c; m = m > d ? m : d;
+    return m;
+  }
+  __host__ __device__ static constexpr int words() { return MulScratch<G, K>::words() + max_all(); }
+};
+
+// Rounded mantissa + exponent for one instance, written by the group.
+template <int G, int PER>
+__device__ __forceinline__ void write_value(const Grp<G> &g, uint32_t *r_exp, uint32_t *r, int n,
+                                            const Rounded<G, PER> &res, uint32_t exp_word) {
+  store_limbs<G, PER>(g, r, n, res);
+  if (g.lane == 0) *r_exp = exp_word;
+}
+
+template <int G>
+__device__ __forceinline__ void write_class(const Grp<G> &g, uint32_t *r_exp, uint32_t cls) {
+  if (g.lane == 0) *r_exp = cls;
+}
+
+template <int G>
+__device__ __forceinline__ void copy_value(const Grp<G> &g, uint32_t *r_exp, uint32_t *r, int n,
+                                           uint32_t exp_word, const uint32_t *src) {
+  for (int i = g.lane; i < n; i += G) r[i] = src[i];
+  if (g.lane == 0) *r_exp = exp_word;
+}
+
+// exponent word from an unbiased exponent (range already checked)
+__device__ __forceinline__ uint32_t exp_word(long long e, uint32_t sign) {
+  return (uint32_t)(2 * ((long long)BIAS + e)) + sign;
+}
+
+// ---------------------------------------------------------------------------------------
+// add / sub.  Reference: fpa_warp_add_sub.h:310-380 (dispatch), :41-125 (same-sign add),
+// :127-282 (effective subtraction).  The aligned sum is formed exactly in n+3 limbs:
+//   X = BIG * 2^64 +- floor(SMALL * 2^(64-d))
+// Bits of SMALL shifted out below the window only matter as a sticky flag; for an
+// effective subtraction one extra unit is subtracted so that the true value lies in
+// (X, X+1) (d > 64 implies at most one bit of cancellation, so 63 guard bits remain).
+// Range: effective add -> +-INF when BIAS+e > 0x7FFFFFFF (:118-119); effective
+// subtraction -> +-TINY when BIAS+e < 5 (:226-227, :272-273).
+template <int G, int K>
+__device__ void op_addsub(const Grp<G> &g, uint32_t *ws, int n, int mode, int is_sub,
+                          uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
+                          uint32_t *r_exp, uint32_t *r) {
+  constexpr int N = G * K;
+  const uint32_t act = c_action[is_sub][classify(a_exp) * 9 + classify(b_exp)];
+  if (act == ACT_COPY_A) { copy_value<G>(g, r_exp, r, n, a_exp, a); return; }
+  if (act == ACT_COPY_B) { copy_value<G>(g, r_exp, r, n, b_exp, b); return; }
+  if (act == ACT_NEG_B) { copy_value<G>(g, r_exp, r, n, b_exp ^ 1u, b); return; }   // 0 - b = -b
+  if (act != ACT_ADD && act != ACT_SUB) { write_class<G>(g, r_exp, act); return; }
+
+  uint32_t *sA = ws + MulScratch<G, K>::words(), *sB = sA + N, *X = sB + N;
+  for (int i = g.lane; i < n; i += G) { sA[i] = a[i]; sB[i] = b[i]; }
+  g.sync();
+  const uint32_t sa = a_exp & 1u, sb = (b_exp & 1u) ^ (uint32_t)is_sub;
+  const long long ea = (long long)(a_exp >> 1) - BIAS, eb = (long long)(b_exp >> 1) - BIAS;
+  const bool eff_sub = sa != sb;
+  bool a_big;
+  if (ea != eb) a_big = ea > eb;
+  else {
+    int c = grp_cmp<G>(g, Ptr{sA, n}, Ptr{sB, n}, n);
+    if (c == 0 && eff_sub) { write_class<G>(g, r_exp, CLS_ZERO); return; }   // exact cancellation
+    a_big = c >= 0;
+  }
+  const uint32_t *big = a_big ? sA : sB, *sml = a_big ? sB : sA;
+  const uint32_t sign = a_big ? sa : sb;
+  const long long ebig = a_big ? ea : eb, esml = a_big ? eb : ea;
+  const long long cap = 32LL * n + 64;
+  const int d = (int)((ebig - esml) > cap ? cap : (ebig - esml));
+  // sticky from SMALL's bits below position d - 64
+  uint32_t lost = 0;
+  if (d > 64) {
+    const int cut = d - 64, full = cut >> 5;
+    for (int i = g.lane; i < full && i < n; i += G) lost |= sml[i];
+    if (g.lane == 0 && (cut & 31) && full < n) lost |= sml[full] & ((1u << (cut & 31)) - 1u);
+    lost = g.ror(lost) != 0;
+  }
+  const int xl = n + 3;
+  Shifted bigs{big, n, 64}, smls{sml, n, 64 - d};
+  if (eff_sub) grp_sub<G>(g, X, bigs, smls, xl, lost);
+  else grp_add<G>(g, X, bigs, smls, xl, 0u);
+  Rounded<G, K + 1> res;
+  if (!grp_round<G, K + 1>(g, X, xl, n, lost, mode, sign, res)) { write_class<G>(g, r_exp, CLS_ZERO); return; }
+  const long long e = ebig - 32LL * n - 64 + res.L + res.ovf;
+  if (!eff_sub && (long long)BIAS + e > 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
+  if (eff_sub && (long long)BIAS + e < 5) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
+  write_value<G, K + 1>(g, r_exp, r, n, res, exp_word(e, sign));
+}
+
+// ---------------------------------------------------------------------------------------
+// mul.  Reference: fpa_warp_mul.h:41-139.  Exact 2n-limb product, one rounding.
+// Range (:124-128): TINY when BIAS+e < 5, INF when BIAS+e > 0x7FFFFFFF.
+template <int G, int K>
+__device__ void op_mul(const Grp<G> &g, uint32_t *ws, int n, int mode,
+                       uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
+                       uint32_t *r_exp, uint32_t *r) {
+  const uint32_t act = c_action[2][classify(a_exp) * 9 + classify(b_exp)];
+  if (act != ACT_MUL) { write_class<G>(g, r_exp, act); return; }
+  MulScratch<G, K> s; s.carve(ws);
+  uint32_t *P = ws + MulScratch<G, K>::words();
+  const int Mp = (n + K - 1) / K, NK = Mp * K;
+  for (int i = g.lane; i < NK; i += G) s.sa[i] = (i < n) ? a[i] : 0u;
+  for (int i = g.lane; i < NK + 2 * K; i += G) { int j = i - K; s.sb[i] = (j >= 0 && j < n) ? b[j] : 0u; }
+  g.sync();
+  grp_mulsq_staged<G, K>(g, P, n, s);
+  const uint32_t sign = (a_exp ^ b_exp) & 1u;
+  Rounded<G, K> res;
+  grp_round<G, K>(g, P, 2 * n, n, 0u, mode, sign, res);
+  const long long e = (long long)(a_exp >> 1) + (long long)(b_exp >> 1) - 2LL * BIAS - 64LL * n + res.L + res.ovf;
+  if ((long long)BIAS + e < 5) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
+  if ((long long)BIAS + e > 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
+  write_value<G, K>(g, r_exp, r, n, res, exp_word(e, sign));
+}
+
+// ---------------------------------------------------------------------------------------
+// Newton level schedule: levels k_0 = 1 < k_1 < ... < k_last = n with
+// k_{j+1} <= 2 k_j - 1 (except 1 -> 2), so the quadratic error term stays below one ulp.
+__device__ __forceinline__ int newton_levels(int n, int *lv) {
+  int tmp[24], c = 0;
+  int k = n;
+  tmp[c++] = k;
+  while (k > 1) {
+    int p = (k + 2) / 2;
+    if (p >= k) p = k - 1;
+    k = p;
+    tmp[c++] = k;
+  }
+  for (int i = 0; i < c; i++) lv[i] = tmp[c - 1 - i];
+  return c;
+}
+
+// m * p as limbs (len+1 limbs) for a small multiplier m in {0, 1, 2, 4}
+struct SmallMul {
+  const uint32_t *p; int len; uint32_t m;
+  __device__ __forceinline__ uint32_t operator()(int i) const {
+    uint32_t v = (i >= 0 && i < len) ? p[i] : 0u, w = (i - 1 >= 0 && i - 1 < len) ? p[i - 1] : 0u;
+    switch (m) {
+      case 0: return 0u;
+      case 1: return v;
+      case 2: return (v << 1) | (w >> 31);
+      default: return (v << 2) | (w >> 30);   // 4
+    }
+  }
+};
+
+// E[0..len) <- |E| (two's complement magnitude); returns the sign
+template <int G>
+__device__ __forceinline__ uint32_t grp_abs(const Grp<G> &g, uint32_t *E, int len) {
+  uint32_t neg = E[len - 1] >> 31;
+  if (neg) grp_sub<G>(g, E, Zero{}, Ptr{E, len}, len, 0u);
+  return neg;
+}
+
+// ---------------------------------------------------------------------------------------
+// div.  Reference: fpa_warp_div.h:127-201.
+//   1. Y ~ 2^(64n)/B by Newton: Y_k' = Y_k*2^(32(k'-k)) + Y_k*E/2^(64k),
+//      E = 2^(32(k+k')) - B_k' * Y_k   (B_k' = top k' limbs of B).
+//   2. Q = floor(A*Y / 2^(32n)), then one exact correction: R = A*2^(32n) - Q*B is formed
+//      from the low n+2 limbs and Q is stepped until 0 <= R < B.
+//   3. X = 2Q + [2R >= B], sticky = R != 0 (2R == B is impossible for a quotient of two
+//      precision-p numbers), rounded once.
+// Range (:189-193): TINY when BIAS+e < 10, INF when BIAS+e >= 0x7FFFFFFF.
+template <int G, int K>
+__device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
+                       uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
+                       uint32_t *r_exp, uint32_t *r, uint32_t *err) {
+  constexpr int N = G * K;
+  const uint32_t act = c_action[3][classify(a_exp) * 9 + classify(b_exp)];
+  if (act != ACT_DIV) { write_class<G>(g, r_exp, act); return; }
+  MulScratch<G, K> s; s.carve(ws);
+  uint32_t *sA = ws + MulScratch<G, K>::words(), *sB = sA + N;
+  uint32_t *Y = sB + N, *Y2 = Y + (N + 4);
+  uint32_t *T = Y2 + (N + 4), *P2 = T + (2 * N + 8);
+  uint32_t *E = P2 + (2 * N + 8), *Q = E + (N + 8), *R = Q + (N + 8);
+  for (int i = g.lane; i < n; i += G) { sA[i] = a[i]; sB[i] = b[i]; }
+  if (g.lane == 0) {
+    uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)b[n - 1];   // level 1: floor((2^64-1)/B_top)
+    Y[0] = (uint32_t)y; Y[1] = (uint32_t)(y >> 32);
+  }
+  g.sync();
+  int lv[24];
+  const int nl = newton_levels(n, lv);
+  for (int li = 1; li < nl; li++) {
+    const int k = lv[li - 1], kp = lv[li];
+    const uint32_t ytop = Y[k];
+    const uint32_t *Bk = sB + (n - kp);
+    // T = B_k' * Y_k  (2k' limbs suffice: k' + k + 1 <= 2k')
+    grp_mulsq<G, K>(g, T, Ptr{Bk, kp}, Ptr{Y, k}, kp, s);
+    grp_add<G>(g, T + k, Ptr{T + k, 2 * kp - k}, SmallMul{Bk, kp, ytop}, 2 * kp - k, 0u);
+    // E = (2^(32(k+k')) - T) mod 2^(32(k'+2))
+    const int le = kp + 2;
+    grp_sub<G>(g, E, Zero{}, Ptr{T, 2 * kp}, le, 0u);
+    if (k + kp < le && g.lane == 0) E[k + kp] += 1u;   // only k == 1: no carry can leave limb le-1
+    g.sync();
+    const uint32_t neg = grp_abs<G>(g, E, le);
+    // M = (Y_k * (|E| >> 32(k-1))) >> 32(k+1)
+    const uint32_t *Et = E + (k - 1);
+    const int lt = le - (k - 1);
+    const int m2 = k > lt ? k : lt;
+    grp_mulsq<G, K>(g, P2, Ptr{Y, k}, Ptr{Et, lt}, m2, s);
+    if (g.lane == 0) { P2[2 * m2] = 0; P2[2 * m2 + 1] = 0; }
+    g.sync();
+    grp_add<G>(g, P2 + k, Ptr{P2 + k, 2 * m2 + 2 - k}, SmallMul{Et, lt, ytop}, 2 * m2 + 2 - k, 0u);
+    // Y_k' = Y_k * 2^(32(k'-k)) +- M
+    Shifted ysh{Y, k + 1, 32 * (kp - k)};
+    Ptr M{P2 + (k + 1), 2 * m2 + 1 - k};
+    if (neg) grp_sub<G>(g, Y2, ysh, M, kp + 1, 0u);
+    else grp_add<G>(g, Y2, ysh, M, kp + 1, 0u);
+    uint32_t *tmp = Y; Y = Y2; Y2 = tmp;
+  }
+  // Q = floor(A * Y / 2^(32n)),  n+1 limbs
+  const uint32_t ytop = Y[n];
+  grp_mulsq<G, K>(g, T, Ptr{sA, n}, Ptr{Y, n}, n, s);
+  if (g.lane == 0) { T[2 * n] = 0; T[2 * n + 1] = 0; }
+  g.sync();
+  grp_add<G>(g, T + n, Ptr{T + n, n + 2}, SmallMul{sA, n, ytop}, n + 2, 0u);
+  grp_copy<G>(g, Q, Ptr{T + n, n + 2}, n + 1);
+  // R = (A * 2^(32n) - Q * B) mod 2^(32(n+2))
+  const uint32_t qtop = Q[n];
+  grp_mulsq<G, K>(g, P2, Ptr{Q, n}, Ptr{sB, n}, n, s);
+  if (g.lane == 0) { P2[2 * n] = 0; P2[2 * n + 1] = 0; P2[2 * n + 2] = 0; }
+  g.sync();
+  grp_add<G>(g, P2 + n, Ptr{P2 + n, n + 3}, SmallMul{sB, n, qtop}, n + 3, 0u);
+  grp_sub<G>(g, R, Shifted{sA, n, 32 * n}, Ptr{P2, 2 * n + 3}, n + 2, 0u);
+  // exact correction: 0 <= R < B
+  int guard = 0;
+  while ((R[n + 1] >> 31) != 0 && guard < 64) {
+    grp_sub<G>(g, Q, Ptr{Q, n + 1}, Zero{}, n + 1, 1u);
+    grp_add<G>(g, R, Ptr{R, n + 2}, Ptr{sB, n}, n + 2, 0u);
+    guard++;
+  }
+  while (grp_cmp<G>(g, Ptr{R, n + 2}, Ptr{sB, n}, n + 2) >= 0 && guard < 64) {
+    grp_add<G>(g, Q, Ptr{Q, n + 1}, Zero{}, n + 1, 1u);
+    grp_sub<G>(g, R, Ptr{R, n + 2}, Ptr{sB, n}, n + 2, 0u);
+    guard++;
+  }
+  if (guard >= 64 && g.lane == 0) atomicOr(err, 1u);
+  const int c2 = grp_cmp<G>(g, ShlBits{R, n + 2, 1}, Ptr{sB, n}, n + 2);
+  const uint32_t rb = c2 >= 0 ? 1u : 0u;
+  const uint32_t sticky = (!grp_is_zero<G>(g, Ptr{R, n + 2}, n + 2) && c2 != 0) ? 1u : 0u;
+  // X = 2Q + rb  (n+2 limbs), reuse E
+  grp_add<G>(g, E, ShlBits{Q, n + 1, 1}, Zero{}, n + 2, rb);
+  const uint32_t sign = (a_exp ^ b_exp) & 1u;
+  Rounded<G, K + 1> res;
+  grp_round<G, K + 1>(g, E, n + 2, n, sticky, mode, sign, res);
+  const long long e = (long long)(a_exp >> 1) - (long long)(b_exp >> 1) - 32LL * n - 1 + res.L + res.ovf;
+  if ((long long)BIAS + e < 10) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
+  if ((long long)BIAS + e >= 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
+  write_value<G, K + 1>(g, r_exp, r, n, res, exp_word(e, sign));
+}
+
+// integer square root of a 64-bit value (bitwise, exact)
+__device__ __forceinline__ uint64_t isqrt64(uint64_t x) {
+  uint64_t r = 0, bit = 1ull << 62;
+  while (bit > x) bit >>= 2;
+  while (bit) {
+    if (x >= r + bit) { x -= r + bit; r = (r >> 1) + bit; }
+    else r >>= 1;
+    bit >>= 2;
+  }
+  return r;
+}
+
+// ---------------------------------------------------------------------------------------
+// sqrt.  Reference: fpa_warp_sqrt.h:195-254 (odd exponents are made even, :218-223).
+//   A_ext = A * 2^(32n) (even e) or A * 2^(32n-1) (odd e), S* = sqrt(A_ext) in [2^(32n-1), 2^(32n)).
+//   1. Z ~ 2^(32k)/sqrt(x) by Newton on 1/sqrt: Z_k' = Z_k*2^(32(k'-k)) + Z_k*E/2^(96k+1),
+//      E = 2^(32(k'+2k)) - X_k' * Z_k^2   (X_k' = top k' limbs of A_ext).
+//   2. S = floor(A * Z / 2^(32n [+1])), one exact correction with R = A_ext - S^2 until
+//      0 <= R <= 2S.
+//   3. X = 2S + [R > S], sticky = R != 0, rounded once (positive).
+template <int G, int K>
+__device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
+                        uint32_t a_exp, const uint32_t *a, uint32_t *r_exp, uint32_t *r, uint32_t *err) {
+  constexpr int N = G * K;
+  const uint32_t act = c_sqrt_action[classify(a_exp)];
+  if (act != ACT_SQRT) { write_class<G>(g, r_exp, act); return; }
+  MulScratch<G, K> s; s.carve(ws);
+  uint32_t *sA = ws + MulScratch<G, K>::words();
+  uint32_t *X2 = sA + N;                       // A_ext, 2n limbs
+  uint32_t *Z = X2 + (2 * N + 4), *Z2 = Z + (N + 4);
+  uint32_t *W = Z2 + (N + 4), *V1 = W + (2 * N + 8), *V2 = V1 + (2 * N + 8), *P = V2 + (2 * N + 8);
+  uint32_t *E = P + (2 * N + 8), *S = E + (2 * N + 8), *R = S + (N + 8);
+  const long long e = (long long)(a_exp >> 1) - BIAS;
+  const int odd = (int)(e & 1);
+  const long long h = (e + odd) / 2;           // exact: e + odd is even
+  for (int i = g.lane; i < n; i += G) sA[i] = a[i];
+  g.sync();
+  grp_copy<G>(g, X2, Shifted{sA, n, 32 * n - odd}, 2 * n);
+  if (g.lane == 0) {
+    uint64_t x1 = (uint64_t)X2[2 * n - 1] << 32;         // top limb of A_ext, in [2^30, 2^32)
+    uint64_t s1 = isqrt64(x1);                             // in [2^31, 2^32)
+    uint64_t z = 0xFFFFFFFFFFFFFFFFull / s1;               // level 1: ~ 2^32 / sqrt(x)
+    Z[0] = (uint32_t)z; Z[1] = (uint32_t)(z >> 32);
+  }
+  g.sync();
+  int lv[24];
+  const int nl = newton_levels(n, lv);
+  for (int li = 1; li < nl; li++) {
+    const int k = lv[li - 1], kp = lv[li];
+    const uint32_t ztop = Z[k];
+    // W = Z_k^2 = Zlow^2 + 2 ztop Zlow 2^(32k) + ztop^2 2^(64k)    (2k+2 limbs)
+    grp_mulsq<G, K>(g, W, Ptr{Z, k}, Ptr{Z, k}, k, s);
+    if (g.lane == 0) { W[2 * k] = 0; W[2 * k + 1] = 0; }
+    g.sync();
+    grp_add<G>(g, W + k, Ptr{W + k, k + 2}, SmallMul{Z, k, 2u * ztop}, k + 2, 0u);
+    if (ztop) {
+      const uint32_t zz = ztop * ztop;
+      grp_add<G>(g, W + 2 * k, Ptr{W + 2 * k, 2}, Ptr{&zz, 1}, 2, 0u);
+    }
+    // V = X_k' * W  mod 2^(32(k'+k+2)), W split at k' limbs
+    const uint32_t *Xk = X2 + (2 * n - kp);
+    const int lw = 2 * k + 2;
+    grp_mulsq<G, K>(g, V1, Ptr{Xk, kp}, Ptr{W, kp < lw ? kp : lw}, kp, s);
+    grp_mulsq<G, K>(g, V2, Ptr{Xk, kp}, Ptr{W + kp, lw - kp}, kp, s);
+    const int lenV = kp + k + 2;
+    if (g.lane == 0) V1[2 * kp] = 0;
+    g.sync();
+    grp_add<G>(g, V1, Ptr{V1, 2 * kp + 1}, Shifted{V2, 2 * kp, 32 * kp}, lenV, 0u);
+    // E = (2^(32(k'+2k)) - V) mod 2^(32 lenV)
+    grp_sub<G>(g, E, Zero{}, Ptr{V1, lenV}, lenV, 0u);
+    if (kp + 2 * k < lenV && g.lane == 0) E[kp + 2 * k] += 1u;   // only k == 1 (top limb)
+    g.sync();
+    const uint32_t neg = grp_abs<G>(g, E, lenV);
+    // M = (Z_k * (|E| >> 32(2k-1))) >> (32(k+1) + 1)
+    const uint32_t *Et = E + (2 * k - 1);
+    const int lt = lenV - (2 * k - 1);
+    const int m2 = k > lt ? k : lt;
+    grp_mulsq<G, K>(g, P, Ptr{Z, k}, Ptr{Et, lt}, m2, s);
+    if (g.lane == 0) { P[2 * m2] = 0; P[2 * m2 + 1] = 0; }
+    g.sync();
+    grp_add<G>(g, P + k, Ptr{P + k, 2 * m2 + 2 - k}, SmallMul{Et, lt, ztop}, 2 * m2 + 2 - k, 0u);
+    Shifted zsh{Z, k + 1, 32 * (kp - k)};
+    Shifted M{P, 2 * m2 + 2, -(32 * (k + 1) + 1)};
+    if (neg) grp_sub<G>(g, Z2, zsh, M, kp + 1, 0u);
+    else grp_add<G>(g, Z2, zsh, M, kp + 1, 0u);
+    uint32_t *tmp = Z; Z = Z2; Z2 = tmp;
+  }
+  // S = floor(A * Z / 2^(32n + odd))   (n+1 limbs)
+  const uint32_t ztop = Z[n];
+  grp_mulsq<G, K>(g, P, Ptr{sA, n}, Ptr{Z, n}, n, s);
+  if (g.lane == 0) { P[2 * n] = 0; P[2 * n + 1] = 0; }
+  g.sync();
+  grp_add<G>(g, P + n, Ptr{P + n, n + 2}, SmallMul{sA, n, ztop}, n + 2, 0u);
+  grp_copy<G>(g, S, Shifted{P, 2 * n + 2, -(32 * n + odd)}, n + 1);
+  // R = (A_ext - S^2) mod 2^(32(n+2)),  S = stop*2^(32n) + Slow
+  const uint32_t stop = S[n];
+  grp_mulsq<G, K>(g, V1, Ptr{S, n}, Ptr{S, n}, n, s);
+  if (g.lane == 0) { V1[2 * n] = 0; V1[2 * n + 1] = 0; V1[2 * n + 2] = 0; }
+  g.sync();
+  grp_add<G>(g, V1 + n, Ptr{V1 + n, n + 3}, SmallMul{S, n, 2u * stop}, n + 3, 0u);
+  if (stop) {
+    const uint32_t ss = stop * stop;
+    grp_add<G>(g, V1 + 2 * n, Ptr{V1 + 2 * n, 3}, Ptr{&ss, 1}, 3, 0u);
+  }
+  grp_sub<G>(g, R, Ptr{X2, 2 * n}, Ptr{V1, 2 * n + 3}, n + 2, 0u);
+  // exact correction: 0 <= R <= 2S
+  int guard = 0;
+  while ((R[n + 1] >> 31) != 0 && guard < 64) {       // R += 2S - 1, S -= 1
+    grp_add<G>(g, R, Ptr{R, n + 2}, ShlBits{S, n + 1, 1}, n + 2, 0u);
+    grp_sub<G>(g, R, Ptr{R, n + 2}, Zero{}, n + 2, 1u);
+    grp_sub<G>(g, S, Ptr{S, n + 1}, Zero{}, n + 1, 1u);
+    guard++;
+  }
+  while (grp_cmp<G>(g, Ptr{R, n + 2}, ShlBits{S, n + 1, 1}, n + 2) > 0 && guard < 64) {   // R -= 2S + 1, S += 1
+    grp_sub<G>(g, R, Ptr{R, n + 2}, ShlBits{S, n + 1, 1}, n + 2, 1u);
+    grp_add<G>(g, S, Ptr{S, n + 1}, Zero{}, n + 1, 1u);
+    guard++;
+  }
+  if (guard >= 64 && g.lane == 0) atomicOr(err, 2u);
+  const uint32_t rb = grp_cmp<G>(g, Ptr{R, n + 2}, Ptr{S, n + 1}, n + 2) > 0 ? 1u : 0u;
+  const uint32_t sticky = grp_is_zero<G>(g, Ptr{R, n + 2}, n + 2) ? 0u : 1u;
+  grp_add<G>(g, E, ShlBits{S, n + 1, 1}, Zero{}, n + 2, rb);
+  Rounded<G, K + 1> res;
+  grp_round<G, K + 1>(g, E, n + 2, n, sticky, mode, 0u, res);
+  const long long er = h - 32LL * n - 1 + res.L + res.ovf;
+  write_value<G, K + 1>(g, r_exp, r, n, res, exp_word(er, 0u));
+}
+
+}  // namespace gfpa

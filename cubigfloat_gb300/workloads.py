@@ -1,0 +1,173 @@
+"""Seeded synthetic operands for the fpa benchmark configurations and tests.
+
+Numbers use the fpa encoding: exponent word 2*(BIAS + e) + sign (classes 0..8 are
+reserved) and n little-endian 32-bit limbs with the top bit set, value = M * 2^(e - 32n).
+All generators take a seed and are deterministic across machines (numpy PCG64).
+"""
+import numpy as np
+
+BIAS = 0x3FFFFFF3
+CLS_ZERO, CLS_NEG_TINY, CLS_POS_TINY, CLS_NEG_INF, CLS_POS_INF, CLS_NAN, CLS_SNAN = 2, 3, 4, 5, 6, 7, 8
+
+
+def exp_word(e, sign):
+    return (2 * (BIAS + np.asarray(e, dtype=np.int64)) + np.asarray(sign, dtype=np.int64)).astype(np.uint32)
+
+
+def decode_exp(w):
+    w = np.asarray(w, dtype=np.int64)
+    return (w >> 1) - BIAS, w & 1
+
+
+def int_to_limbs(x, n):
+    return np.frombuffer(int(x).to_bytes(4 * n, "little"), dtype=np.uint32).copy()
+
+
+def limbs_to_int(limbs):
+    return int.from_bytes(np.ascontiguousarray(limbs, dtype=np.uint32).tobytes(), "little")
+
+
+def uniform(rng, count, n, emin, emax, signs=True):
+    """Uniform random mantissas (top bit set), exponents uniform in [emin, emax]."""
+    limbs = rng.integers(0, 1 << 32, size=(count, n), dtype=np.uint64).astype(np.uint32)
+    limbs[:, n - 1] |= np.uint32(0x80000000)
+    e = rng.integers(emin, emax + 1, size=count)
+    s = rng.integers(0, 2, size=count) if signs else np.zeros(count, dtype=np.int64)
+    return exp_word(e, s), limbs
+
+
+def reference_style(rng, count, n, shift_frac=5 / 8):
+    """The reference test generator's pattern (tests.c:173-181, 815-830): limbs drawn from
+    {0, 1, 0x7FFFFFFF, 0x80000000, 0xFFFFFFFF}, normalised, exponent offset drawn as the
+    difference of two uniform values below 5/8 of the precision, random sign."""
+    vals = np.array([0, 1, 0x7FFFFFFF, 0x80000000, 0xFFFFFFFF], dtype=np.uint32)
+    raw = vals[rng.integers(0, 5, size=(count, n))]
+    exps = np.zeros(count, dtype=np.uint32)
+    limbs = np.zeros((count, n), dtype=np.uint32)
+    p = 32 * n
+    span = max(1, int(p * shift_frac))
+    for i in range(count):
+        m = limbs_to_int(raw[i])
+        if m == 0:
+            m = 1 << (p - 1)
+        L = m.bit_length()
+        m <<= p - L
+        e = L - p + int(rng.integers(0, span)) - int(rng.integers(0, span))
+        limbs[i] = int_to_limbs(m, n)
+        exps[i] = 2 * (BIAS + e) + int(rng.integers(0, 2))
+    return exps, limbs
+
+
+# ---- near-halfway constructions (config 2's 5% hard cases) ---------------------------
+
+def _rand_bits(rng, bits):
+    """random integer with exactly `bits` significant bits"""
+    nb = (bits + 31) // 32
+    words = rng.integers(0, 1 << 32, size=nb, dtype=np.uint64)
+    x = 0
+    for w in words[::-1]:
+        x = (x << 32) | int(w)
+    x &= (1 << bits) - 1
+    return x | (1 << (bits - 1))
+
+
+def mul_near_half(rng, n):
+    """Mantissas A, B (p = 32n bits) whose exact product has its bits below the rounding
+    position equal to 10...0 (an exact tie) or 10...0 +- 1."""
+    p = 32 * n
+    delta = int(rng.integers(-1, 2))
+    for _ in range(1000):
+        A = _rand_bits(rng, p) | 1
+        if rng.integers(0, 2):
+            # product of 2p-1 bits: tail = low p-1 bits
+            mod = 1 << (p - 1)
+            T = (1 << (p - 2)) + delta
+            B = (1 << (p - 1)) + (T * pow(A, -1, mod)) % mod
+            want = 2 * p - 1
+        else:
+            # product of 2p bits: tail = low p bits
+            mod = 1 << p
+            T = (1 << (p - 1)) + delta
+            B = (T * pow(A, -1, mod)) % mod
+            want = 2 * p
+        if B >> (p - 1) == 1 and (A * B).bit_length() == want:
+            return A, B
+    raise RuntimeError("no near-halfway pair found")
+
+
+def div_near_exact(rng, n):
+    """a = q*b +- 1 ulp with q and b of p/2 bits: the quotient sits within ~2^-p ulp of a
+    representable value."""
+    p = 32 * n
+    h = max(1, p // 2 - 1)
+    while True:
+        q = _rand_bits(rng, h)
+        b = _rand_bits(rng, h) | 1
+        qb = q * b
+        A = qb << (p - qb.bit_length())
+        A += int(rng.integers(-1, 2))
+        if A.bit_length() == p:
+            return A, b << (p - b.bit_length())
+
+
+def sqrt_near_exact(rng, n):
+    """x = s^2 +- 1 ulp with s of at most p/2 bits (the reference's pattern, tests.c:894-906).
+    Returns the mantissa and the exponent parity that makes s^2 an exact square."""
+    p = 32 * n
+    s = _rand_bits(rng, max(1, p // 2 - 1))
+    sq = s * s
+    A = (sq << (p - sq.bit_length())) + int(rng.integers(-1, 2))
+    if A.bit_length() != p:
+        A = sq << (p - sq.bit_length())
+    # x = A * 2^(e - p) = sq * 2^(e - L): exact square when e - L is even
+    return A, sq.bit_length() & 1
+
+
+def config2(op, seed, count=1 << 20, n=128, hard_frac=0.05, pool=1024):
+    """4096-bit mul/div/sqrt operands: uniform mantissas, e in [-1000, 1000]; nonzero
+    divisors, positive sqrt arguments; `hard_frac` of the instances are near-halfway
+    (mul) or near-exact (div, sqrt) cases drawn from a pool of distinct constructions."""
+    rng = np.random.default_rng(seed)
+    a_exps, a_limbs = uniform(rng, count, n, -1000, 1000, signs=(op != "sqrt"))
+    b_exps, b_limbs = uniform(rng, count, n, -1000, 1000, signs=True)
+    nh = int(count * hard_frac)
+    if nh:
+        idx = rng.choice(count, size=nh, replace=False)
+        npool = min(pool, nh)
+        cases = []
+        for _ in range(npool):
+            if op == "mul":
+                cases.append(mul_near_half(rng, n))
+            elif op == "div":
+                cases.append(div_near_exact(rng, n))
+            else:
+                cases.append(sqrt_near_exact(rng, n))
+        for j, i in enumerate(idx):
+            A, B = cases[j % npool]
+            a_limbs[i] = int_to_limbs(A, n)
+            if op == "sqrt":
+                e = 2 * int(rng.integers(-500, 500)) + B      # B = required exponent parity
+                a_exps[i] = 2 * (BIAS + e)
+            else:
+                b_limbs[i] = int_to_limbs(B, n)
+    return (a_exps, a_limbs), (b_exps, b_limbs)
+
+
+def config1(seed, count=65536, n=32):
+    """1024-bit add/mul operands: uniform mantissas, e in [-64, 64], random signs."""
+    rng = np.random.default_rng(seed)
+    a = uniform(rng, count, n, -64, 64)
+    b = uniform(rng, count, n, -64, 64)
+    return a, b
+
+
+def specials(n):
+    """One operand of each class plus +-1.0 and +-0.75, for special-value tables."""
+    one = np.zeros(n, dtype=np.uint32)
+    one[n - 1] = 0x80000000
+    tq = np.zeros(n, dtype=np.uint32)
+    tq[n - 1] = 0xC0000000
+    exps = [exp_word(1, 0), exp_word(1, 1), exp_word(0, 0), exp_word(0, 1),
+            CLS_ZERO, CLS_NEG_TINY, CLS_POS_TINY, CLS_NEG_INF, CLS_POS_INF, CLS_NAN, CLS_SNAN]
+    limbs = [one, one, tq, tq] + [np.zeros(n, dtype=np.uint32)] * 7
+    return np.array(exps, dtype=np.uint32), np.stack(limbs)

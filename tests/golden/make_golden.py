@@ -1,0 +1,75 @@
+"""Generate the committed golden fixtures: MPFR 4.2.1 results for seeded operands.
+
+Run from the repository root:  python tests/golden/make_golden.py
+Writes tests/golden/fixtures/<op>_n<limbs>.npz with the operands (a_*, b_*) and, for each
+rounding mode m = 0..4, the MPFR result (r_exps[m], r_limbs[m]).  Operand sets per file:
+uniform mantissas, the reference test generator's limb pattern (tests.c:173-181) and the
+near-halfway / near-exact constructions of config 2.
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+import gold  # noqa: E402
+from cubigfloat_gb300 import workloads as W  # noqa: E402
+
+OPS = ["add", "sub", "mul", "div", "sqrt"]
+SIZES = {1: 24, 8: 24, 32: 24, 33: 24, 64: 16, 128: 16, 160: 6}
+OUT = os.path.join(ROOT, "tests", "golden", "fixtures")
+
+
+def operands(op, n, count, seed):
+    rng = np.random.default_rng(seed)
+    k1 = count // 2
+    k2 = count // 4
+    k3 = count - k1 - k2
+    ae, al = W.uniform(rng, k1, n, -200, 200)
+    be, bl = W.uniform(rng, k1, n, -200, 200)
+    re_a, rl_a = W.reference_style(rng, k2, n)
+    re_b, rl_b = W.reference_style(rng, k2, n)
+    he_a = np.zeros(k3, np.uint32); hl_a = np.zeros((k3, n), np.uint32)
+    he_b = np.zeros(k3, np.uint32); hl_b = np.zeros((k3, n), np.uint32)
+    for i in range(k3):
+        if op in ("mul", "add", "sub"):
+            A, B = W.mul_near_half(rng, n)
+        elif op == "div":
+            A, B = W.div_near_exact(rng, n)
+        else:
+            A, par = W.sqrt_near_exact(rng, n)
+            B = A
+        hl_a[i] = W.int_to_limbs(A, n); hl_b[i] = W.int_to_limbs(B, n)
+        ea = int(rng.integers(-20, 20)); eb = int(rng.integers(-20, 20))
+        if op == "sqrt":
+            ea = 2 * (ea // 2) + par
+        he_a[i] = W.exp_word(ea, 0 if op == "sqrt" else int(rng.integers(0, 2)))
+        he_b[i] = W.exp_word(eb, int(rng.integers(0, 2)))
+    a_exps = np.concatenate([ae, re_a, he_a]); a_limbs = np.concatenate([al, rl_a, hl_a])
+    b_exps = np.concatenate([be, re_b, he_b]); b_limbs = np.concatenate([bl, rl_b, hl_b])
+    if op == "sqrt":
+        a_exps = a_exps & ~np.uint32(1)
+    return a_exps, a_limbs, b_exps, b_limbs
+
+
+def main():
+    os.makedirs(OUT, exist_ok=True)
+    for oi, op in enumerate(OPS):
+        for n, count in SIZES.items():
+            a_exps, a_limbs, b_exps, b_limbs = operands(op, n, count, seed=1000 * oi + n)
+            r_e, r_l = [], []
+            for mode in range(5):
+                e, l = gold.run(oi, n, mode, a_exps, a_limbs, b_exps, b_limbs)
+                l[e <= 8] = 0
+                r_e.append(e); r_l.append(l)
+            np.savez_compressed(os.path.join(OUT, f"{op}_n{n}.npz"), op=oi, n=n,
+                                a_exps=a_exps, a_limbs=a_limbs, b_exps=b_exps, b_limbs=b_limbs,
+                                r_exps=np.stack(r_e), r_limbs=np.stack(r_l),
+                                mpfr_version=gold.version())
+    print("wrote", len(os.listdir(OUT)), "fixtures to", OUT)
+
+
+if __name__ == "__main__":
+    main()
