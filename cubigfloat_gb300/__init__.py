@@ -77,6 +77,7 @@ def lib():
         "fpa_gb300_set_config": (i32, [u32, i32]),
         "fpa_gb300_get_config": (i32, [u32]),
         "fpa_gb300_version": (ctypes.c_char_p, []),
+        "fpa_gb300_measure_imad_peak": (i32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -225,3 +226,12 @@ def set_config(limbs, cfg):
 
 def get_config(limbs):
     return lib().fpa_gb300_get_config(limbs)
+
+
+def measure_imad_peak():
+    """(mad.lo.u32/s, mad.hi.u32/s) measured on the current GPU."""
+    lo, hi = ctypes.c_double(), ctypes.c_double()
+    rc = lib().fpa_gb300_measure_imad_peak(ctypes.byref(lo), ctypes.byref(hi))
+    if rc != fpa_success:
+        raise FpaError(f"fpa_gb300_measure_imad_peak -> {rc}")
+    return lo.value, hi.value

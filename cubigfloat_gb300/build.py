@@ -42,6 +42,7 @@ def _units():
         units.append(("fpa_kernels.cu", [f"-DGFPA_CFG={c}"], f"fpa_kernels_cfg{c}.o"))
     units.append(("fpa_misc.cu", [], "fpa_misc.o"))
     units.append(("fpa_api.cu", [], "fpa_api.o"))
+    units.append(("fpa_probe.cu", [], "fpa_probe.o"))
     units.append(("fpa_batch.cu", [], "fpa_batch.o"))
     units.append(("fpa_serve.cu", [], "fpa_serve.o"))
     return [u for u in units if os.path.exists(os.path.join(CSRC, u[0]))]

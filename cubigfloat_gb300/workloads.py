@@ -123,10 +123,11 @@ def sqrt_near_exact(rng, n):
     return A, sq.bit_length() & 1
 
 
-def config2(op, seed, count=1 << 20, n=128, hard_frac=0.05, pool=1024):
+def config2(op, seed, count=1 << 20, n=128, hard_frac=0.05, pool=256):
     """4096-bit mul/div/sqrt operands: uniform mantissas, e in [-1000, 1000]; nonzero
     divisors, positive sqrt arguments; `hard_frac` of the instances are near-halfway
-    (mul) or near-exact (div, sqrt) cases drawn from a pool of distinct constructions."""
+    (mul) or near-exact (div, sqrt) cases drawn from a pool of distinct constructions
+    (each placed with its own random exponents and signs)."""
     rng = np.random.default_rng(seed)
     a_exps, a_limbs = uniform(rng, count, n, -1000, 1000, signs=(op != "sqrt"))
     b_exps, b_limbs = uniform(rng, count, n, -1000, 1000, signs=True)
@@ -134,22 +135,17 @@ def config2(op, seed, count=1 << 20, n=128, hard_frac=0.05, pool=1024):
     if nh:
         idx = rng.choice(count, size=nh, replace=False)
         npool = min(pool, nh)
-        cases = []
-        for _ in range(npool):
-            if op == "mul":
-                cases.append(mul_near_half(rng, n))
-            elif op == "div":
-                cases.append(div_near_exact(rng, n))
-            else:
-                cases.append(sqrt_near_exact(rng, n))
-        for j, i in enumerate(idx):
-            A, B = cases[j % npool]
-            a_limbs[i] = int_to_limbs(A, n)
-            if op == "sqrt":
-                e = 2 * int(rng.integers(-500, 500)) + B      # B = required exponent parity
-                a_exps[i] = 2 * (BIAS + e)
-            else:
-                b_limbs[i] = int_to_limbs(B, n)
+        make = {"mul": mul_near_half, "div": div_near_exact, "sqrt": sqrt_near_exact}[op]
+        cases = [make(rng, n) for _ in range(npool)]
+        pa = np.stack([int_to_limbs(A, n) for A, _ in cases])
+        pick = np.arange(nh) % npool
+        a_limbs[idx] = pa[pick]
+        if op == "sqrt":
+            parity = np.array([par for _, par in cases], dtype=np.int64)[pick]   # exponent parity for s^2
+            e = 2 * rng.integers(-500, 500, size=nh) + parity
+            a_exps[idx] = exp_word(e, 0)
+        else:
+            b_limbs[idx] = np.stack([int_to_limbs(B, n) for _, B in cases])[pick]
     return (a_exps, a_limbs), (b_exps, b_limbs)
 
 

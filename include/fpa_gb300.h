@@ -46,6 +46,10 @@ fpa_result fpa_gb300_config_shape(int cfg, uint32_t *lanes, uint32_t *tile_limbs
 fpa_result fpa_gb300_set_config(uint32_t limbs, int cfg);
 int fpa_gb300_get_config(uint32_t limbs);
 
+/* Measured integer multiply-add throughput of the current GPU (mad.lo.u32 and mad.hi.u32
+ * per second over all SMs): the roofline denominator for the multiply-bound operations. */
+fpa_result fpa_gb300_measure_imad_peak(double *mad_lo_per_s, double *mad_hi_per_s);
+
 const char *fpa_gb300_version(void);
 
 #ifdef __cplusplus

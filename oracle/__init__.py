@@ -105,3 +105,53 @@ def build_ref(reference_root=os.environ.get("FPA_REFERENCE_ROOT", "/root/referen
     subprocess.run([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-DGPU", "-O3",
                     "-o", REF_CUBIN, src], check=True, capture_output=True)
     return REF_CUBIN
+
+
+RUNNER_SRC = os.path.join(HERE, "ref_runner.c")
+RUNNER_LIB = os.path.join(BUILD, "libref_runner.so")
+_runner = None
+
+
+def ref_gpu_available():
+    return os.path.exists(REF_CUBIN)
+
+
+def _runner_lib():
+    global _runner
+    if _runner is None:
+        os.makedirs(BUILD, exist_ok=True)
+        if not os.path.exists(RUNNER_LIB) or os.path.getmtime(RUNNER_LIB) < os.path.getmtime(RUNNER_SRC):
+            subprocess.run(["gcc", "-O2", "-shared", "-fPIC", RUNNER_SRC, "-o", RUNNER_LIB, "-ldl"], check=True)
+        L = ctypes.CDLL(RUNNER_LIB)
+        vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
+        L.ref_load.restype = i32
+        L.ref_load.argtypes = [ctypes.c_char_p]
+        L.ref_run.restype = i32
+        L.ref_run.argtypes = [ctypes.c_char_p, u32, u32, i32, vp, vp, vp, vp, vp, vp, i32,
+                              ctypes.POINTER(ctypes.c_float)]
+        rc = L.ref_load(REF_CUBIN.encode())
+        if rc != 0:
+            raise RuntimeError(f"ref_load failed rc={rc}")
+        _runner = L
+    return _runner
+
+
+def ref_gpu_run(op, n, mode, a_exps, a_limbs, b_exps=None, b_limbs=None, repeat=1):
+    """Run the reference's own kernel for `op` ("add".."sqrt") on the GPU.
+    Returns (r_exps, r_limbs, ms_per_launch)."""
+    L = _runner_lib()
+    a_exps = np.ascontiguousarray(a_exps, dtype=np.uint32)
+    a_limbs = np.ascontiguousarray(a_limbs, dtype=np.uint32).reshape(-1, n)
+    count = a_exps.size
+    if op != "sqrt":
+        b_exps = np.ascontiguousarray(b_exps, dtype=np.uint32)
+        b_limbs = np.ascontiguousarray(b_limbs, dtype=np.uint32).reshape(-1, n)
+    r_exps = np.zeros(count, dtype=np.uint32)
+    r_limbs = np.zeros((count, n), dtype=np.uint32)
+    ms = ctypes.c_float()
+    rc = L.ref_run(op.encode(), 32 * n, count, mode, _p(r_exps), _p(r_limbs), _p(a_exps), _p(a_limbs),
+                   _p(b_exps) if op != "sqrt" else None, _p(b_limbs) if op != "sqrt" else None,
+                   repeat, ctypes.byref(ms))
+    if rc != 0:
+        raise RuntimeError(f"ref_run({op}) rc={rc}")
+    return r_exps, r_limbs, ms.value
