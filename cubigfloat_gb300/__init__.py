@@ -78,6 +78,14 @@ def lib():
         "fpa_gb300_get_config": (i32, [u32]),
         "fpa_gb300_version": (ctypes.c_char_p, []),
         "fpa_gb300_measure_imad_peak": (i32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+        "fpa_batch_create": (i32, [ctypes.POINTER(vp), vp, u64]),
+        "fpa_batch_run": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
+        "fpa_batch_capture": (i32, [vp, vp, vp, vp, vp, vp, vp]),
+        "fpa_batch_graph_launch": (i32, [vp, vp]),
+        "fpa_batch_info": (i32, [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]),
+        "fpa_batch_destroy": (i32, [vp]),
+        "fpa_gb300_set_op_config": (i32, [i32, u32, i32]),
+        "fpa_gb300_get_op_config": (i32, [i32, u32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -235,3 +243,57 @@ def measure_imad_peak():
     if rc != fpa_success:
         raise FpaError(f"fpa_gb300_measure_imad_peak -> {rc}")
     return lo.value, hi.value
+
+
+def set_op_config(op, limbs, cfg):
+    return lib().fpa_gb300_set_op_config(op, limbs, cfg)
+
+
+def get_op_config(op, limbs):
+    return lib().fpa_gb300_get_op_config(op, limbs)
+
+
+# fpa_gb300.h: fpa_batch_desc (32 bytes)
+BATCH_DESC = np.dtype([("op", "u1"), ("mode", "u1"), ("limbs", "<u2"), ("reserved", "<u4"),
+                       ("r_off", "<u8"), ("a_off", "<u8"), ("b_off", "<u8")])
+
+
+class Batch:
+    """fpa_batch_t: a planned mixed batch (descriptors are a BATCH_DESC array)."""
+
+    def __init__(self, descs):
+        descs = np.ascontiguousarray(descs, dtype=BATCH_DESC)
+        self.count = descs.size
+        self.h = ctypes.c_void_p()
+        rc = lib().fpa_batch_create(ctypes.byref(self.h), descs.ctypes.data_as(ctypes.c_void_p), self.count)
+        if rc != fpa_success:
+            raise FpaError(f"fpa_batch_create -> {rc}")
+
+    def run(self, r_exps, r_limbs, a_exps, a_limbs, b_exps=0, b_limbs=0, stream=0):
+        v = ctypes.c_void_p
+        return lib().fpa_batch_run(self.h, v(r_exps), v(r_limbs), v(a_exps), v(a_limbs), v(b_exps), v(b_limbs),
+                                   v(stream))
+
+    def capture(self, r_exps, r_limbs, a_exps, a_limbs, b_exps=0, b_limbs=0):
+        v = ctypes.c_void_p
+        return lib().fpa_batch_capture(self.h, v(r_exps), v(r_limbs), v(a_exps), v(a_limbs), v(b_exps), v(b_limbs))
+
+    def graph_launch(self, stream=0):
+        return lib().fpa_batch_graph_launch(self.h, ctypes.c_void_p(stream))
+
+    def info(self):
+        t = (ctypes.c_uint32 * 3)()
+        k = ctypes.c_uint32()
+        lib().fpa_batch_info(self.h, t, ctypes.byref(k))
+        return list(t), k.value
+
+    def destroy(self):
+        if self.h:
+            lib().fpa_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

@@ -12,6 +12,7 @@
 #include "../../include/fpa_gb300.h"
 #include "fpa_launch.h"
 #include "fpa_misc.h"
+#include "fpa_batch.h"
 
 namespace {
 
@@ -20,10 +21,36 @@ struct State {
   int device = -1;
   int sms = 0;
   uint32_t *err = nullptr;                // device error word
-  int8_t cfg_override[GFPA_MAX_LIMBS + 1];
+  int8_t cfg_override[5][GFPA_MAX_LIMBS + 1];   // per operation and limb count, -1 = default
   State() { memset(cfg_override, -1, sizeof cfg_override); }
 };
 State g_state;
+
+bool ctx(int &sms, uint32_t *&err);
+
+}  // namespace
+
+bool gfpa_context(int *sms, uint32_t **err) {
+  int s; uint32_t *e;
+  if (!ctx(s, e)) return false;
+  if (sms) *sms = s;
+  if (err) *err = e;
+  return true;
+}
+
+static bool cfg_fits(int c, uint32_t n) {
+  const uint32_t cap = (uint32_t)(gfpa_cfg_G[c] * gfpa_cfg_K[c]);
+  return cap >= n && cap >= 4;
+}
+
+int gfpa_cfg_for_op(int op, uint32_t n) {
+  if (op < 0 || op > 4 || n == 0 || n > GFPA_MAX_LIMBS) return -1;
+  int c = g_state.cfg_override[op][n];
+  if (c >= 0 && cfg_fits(c, n)) return c;
+  return gfpa_default_cfg(n);
+}
+
+namespace {
 
 // per-process device context (the current device at first use)
 bool ctx(int &sms, uint32_t *&err) {
@@ -46,11 +73,6 @@ bool valid_precision(uint32_t precision) {
   return precision >= 32 && precision <= 32u * GFPA_MAX_LIMBS && precision % 32 == 0;
 }
 
-int cfg_for(uint32_t n) {
-  int c = (n <= GFPA_MAX_LIMBS) ? g_state.cfg_override[n] : -1;
-  if (c >= 0 && (uint32_t)(gfpa_cfg_G[c] * gfpa_cfg_K[c]) >= n && (n >= 4 || gfpa_cfg_G[c] * gfpa_cfg_K[c] >= 4)) return c;
-  return gfpa_default_cfg(n);
-}
 
 fpa_result launch_elementwise(int op, uint32_t precision, uint64_t count, int mode, uint32_t *r_exps, uint32_t *r_limbs,
                               const uint32_t *a_exps, const uint32_t *a_limbs, const uint32_t *b_exps,
@@ -66,7 +88,7 @@ fpa_result launch_elementwise(int op, uint32_t precision, uint64_t count, int mo
   args.a_exps = a_exps; args.a_limbs = a_limbs;
   args.b_exps = (op == 4) ? a_exps : b_exps; args.b_limbs = (op == 4) ? a_limbs : b_limbs;
   args.err = err;
-  int cfg = cfg_for(args.n);
+  int cfg = gfpa_cfg_for_op(op, args.n);
   if (cfg < 0) return fpa_invalid_precisions;
   return gfpa_launch(cfg, op, &args, stream, sms) == cudaSuccess ? fpa_success : fpa_device_error;
 }
@@ -251,19 +273,27 @@ fpa_result fpa_gb300_config_shape(int cfg, uint32_t *lanes, uint32_t *tile_limbs
   return fpa_success;
 }
 
-fpa_result fpa_gb300_set_config(uint32_t limbs, int cfg) {
+fpa_result fpa_gb300_set_op_config(fpa_op op, uint32_t limbs, int cfg) {
+  if ((int)op < 0 || (int)op > 4) return fpa_math_error;
   if (limbs == 0 || limbs > GFPA_MAX_LIMBS) return fpa_invalid_precisions;
   if (cfg < -1 || cfg >= GFPA_NUM_CFGS) return fpa_math_error;
-  if (cfg >= 0 && (uint32_t)(gfpa_cfg_G[cfg] * gfpa_cfg_K[cfg]) < limbs) return fpa_invalid_precisions;
+  if (cfg >= 0 && !cfg_fits(cfg, limbs)) return fpa_invalid_precisions;
   std::lock_guard<std::mutex> lk(g_state.mu);
-  g_state.cfg_override[limbs] = (int8_t)cfg;
+  g_state.cfg_override[(int)op][limbs] = (int8_t)cfg;
   return fpa_success;
 }
 
-int fpa_gb300_get_config(uint32_t limbs) {
-  if (limbs == 0 || limbs > GFPA_MAX_LIMBS) return -1;
-  return cfg_for(limbs);
+int fpa_gb300_get_op_config(fpa_op op, uint32_t limbs) { return gfpa_cfg_for_op((int)op, limbs); }
+
+fpa_result fpa_gb300_set_config(uint32_t limbs, int cfg) {
+  for (int op = 0; op < 5; op++) {
+    fpa_result r = fpa_gb300_set_op_config((fpa_op)op, limbs, cfg);
+    if (r != fpa_success) return r;
+  }
+  return fpa_success;
 }
+
+int fpa_gb300_get_config(uint32_t limbs) { return gfpa_cfg_for_op(2, limbs); }
 
 const char *fpa_gb300_version(void) { return "fpa_gb300 0.1 (sm_103a)"; }
 

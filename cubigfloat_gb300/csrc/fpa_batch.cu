@@ -1,0 +1,270 @@
+// fpa_batch.cu -- host side of the batched form: one submission runs many operations of
+// mixed type and precision.
+//
+// Plan: every descriptor gets a lane-group configuration (autotuned table, per operation
+// and limb count) and therefore a register class; descriptors are sorted by (class,
+// configuration, operation, limbs descending) and cut into tasks of about two operations
+// per lane group of a CTA, ordered longest-first within each class (longest processing
+// time first keeps the persistent CTAs evenly loaded to the end).
+// Run: one persistent kernel per non-empty class (fpa_batch_kernels.cu), class 0 on the
+// caller's stream and classes 1 and 2 on forked side streams so they share the GPU
+// concurrently; a run can be captured once as a CUDA graph and replayed with one launch.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <vector>
+#include "../../include/fpa_gb300.h"
+#include "fpa_ops.cuh"
+#include "fpa_launch.h"
+#include "fpa_batch.h"
+
+using namespace gfpa;
+
+namespace {
+
+// shared-memory words one warp needs for (configuration, operation)
+int warp_words_for(int cfg, int op) {
+#define GFPA_W(CFG, GG, KK)                                                                   \
+  if (cfg == CFG) {                                                                          \
+    switch (op) {                                                                            \
+      case OP_ADD: case OP_SUB: return (32 / GG) * OpWords<OP_ADD, GG, KK>::aligned();         \
+      case OP_MUL: return (32 / GG) * OpWords<OP_MUL, GG, KK>::aligned();                       \
+      case OP_DIV: return (32 / GG) * OpWords<OP_DIV, GG, KK>::aligned();                       \
+      default: return (32 / GG) * OpWords<OP_SQRT, GG, KK>::aligned();                          \
+    }                                                                                        \
+  }
+  GFPA_W(0, 4, 2) GFPA_W(1, 8, 2) GFPA_W(2, 8, 4) GFPA_W(3, 16, 4) GFPA_W(4, 32, 4) GFPA_W(5, 32, 8) GFPA_W(6, 32, 16)
+  GFPA_W(7, 16, 8) GFPA_W(8, 8, 16) GFPA_W(9, 16, 16)
+#undef GFPA_W
+  return 0;
+}
+
+// relative cost used to order tasks (products plus fixed per-operation work)
+double op_weight(int op, int n) {
+  const double nn = (double)n * n;
+  switch (op) {
+    case OP_ADD: case OP_SUB: return 64.0 * n + 2000.0;
+    case OP_MUL: return nn + 4000.0;
+    case OP_DIV: return 4.0 * nn + 40000.0;
+    default: return 6.0 * nn + 60000.0;
+  }
+}
+
+cudaError_t prepare(int c, size_t smem, int *per_sm) {
+  switch (c) {
+    case 0: return gfpa_batch_prepare0(smem, per_sm);
+    case 1: return gfpa_batch_prepare1(smem, per_sm);
+    default: return gfpa_batch_prepare2(smem, per_sm);
+  }
+}
+
+cudaError_t launch(int c, const BatchArgs *a, int grid, size_t smem, cudaStream_t st) {
+  switch (c) {
+    case 0: return gfpa_batch_launch0(a, grid, smem, st);
+    case 1: return gfpa_batch_launch1(a, grid, smem, st);
+    default: return gfpa_batch_launch2(a, grid, smem, st);
+  }
+}
+
+}  // namespace
+
+struct fpa_batch_s {
+  uint64_t count = 0;
+  fpa_batch_desc *d_descs = nullptr;
+  uint32_t *d_order = nullptr;
+  BatchTask *d_tasks = nullptr;
+  uint32_t *d_counters = nullptr;     // one per class
+  uint32_t ntasks[3] = {0, 0, 0}, task_base[3] = {0, 0, 0};
+  uint32_t warp_words[3] = {0, 0, 0};
+  int grid[3] = {0, 0, 0};
+  size_t smem[3] = {0, 0, 0};
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" fpa_result fpa_batch_create(fpa_batch_t *out, const fpa_batch_desc *descs, uint64_t count) {
+  if (!out) return fpa_math_error;
+  *out = nullptr;
+  if (count > 0xFFFFFFFFull) return fpa_invalid_counts;
+  if (count && !descs) return fpa_math_error;
+  int sms;
+  if (!gfpa_context(&sms, nullptr)) return fpa_device_error;
+  std::vector<uint32_t> order(count);
+  std::vector<uint16_t> key(count);
+  std::vector<uint8_t> cls(count);
+  for (uint64_t i = 0; i < count; i++) {
+    const fpa_batch_desc &d = descs[i];
+    if (d.op > 4 || d.mode > 4) return fpa_math_error;
+    if (d.limbs == 0 || d.limbs > GFPA_MAX_LIMBS) return fpa_invalid_precisions;
+    const int cfg = gfpa_cfg_for_op(d.op, d.limbs);
+    if (cfg < 0) return fpa_invalid_precisions;
+    key[i] = (uint16_t)(cfg * 5 + d.op);
+    cls[i] = (uint8_t)gfpa_class_of(cfg, d.op);
+    order[i] = (uint32_t)i;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+    if (cls[x] != cls[y]) return cls[x] < cls[y];
+    if (key[x] != key[y]) return key[x] < key[y];
+    return descs[x].limbs > descs[y].limbs;
+  });
+  std::vector<BatchTask> tasks[3];
+  std::vector<double> cost[3];
+  uint64_t i = 0;
+  while (i < count) {
+    uint64_t j = i;
+    const uint16_t k = key[order[i]];
+    while (j < count && key[order[j]] == k) j++;
+    const int cfg = k / 5, op = k % 5, c = gfpa_class_of(cfg, op);
+    const int groups = (gfpa_class_threads[c] / 32) * (32 / gfpa_cfg_G[cfg]);
+    const uint64_t chunk = (uint64_t)groups * 2;
+    for (uint64_t s = i; s < j; s += chunk) {
+      BatchTask t;
+      t.key = k; t.pad = 0; t.first = (uint32_t)s;
+      t.count = (uint32_t)std::min<uint64_t>(chunk, j - s);
+      double w = 0;
+      for (uint64_t q = s; q < s + t.count; q++) w += op_weight(op, descs[order[q]].limbs);
+      tasks[c].push_back(t);
+      cost[c].push_back(w / groups);
+    }
+    i = j;
+  }
+  fpa_batch_s *b = new fpa_batch_s();
+  b->count = count;
+  std::vector<BatchTask> all;
+  for (int c = 0; c < 3; c++) {
+    std::vector<size_t> idx(tasks[c].size());
+    for (size_t q = 0; q < idx.size(); q++) idx[q] = q;
+    std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return cost[c][x] > cost[c][y]; });
+    b->task_base[c] = (uint32_t)all.size();
+    b->ntasks[c] = (uint32_t)idx.size();
+    uint32_t ww = 0;
+    for (size_t q : idx) {
+      all.push_back(tasks[c][q]);
+      ww = std::max<uint32_t>(ww, (uint32_t)warp_words_for(tasks[c][q].key / 5, tasks[c][q].key % 5));
+    }
+    b->warp_words[c] = ww;
+    b->smem[c] = (size_t)(gfpa_class_threads[c] / 32) * ww * 4;
+    if (b->smem[c] > 227 * 1024) { fpa_batch_destroy(b); return fpa_device_error; }
+    if (b->ntasks[c]) {
+      int per = 0;
+      if (prepare(c, b->smem[c], &per) != cudaSuccess) { fpa_batch_destroy(b); return fpa_device_error; }
+      if (per < 1) per = 1;
+      b->grid[c] = (int)std::min<uint64_t>((uint64_t)per * sms, b->ntasks[c]);
+    }
+  }
+  bool ok = true;
+  ok = ok && cudaMalloc(&b->d_descs, std::max<size_t>(1, count) * sizeof(fpa_batch_desc)) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_order, std::max<size_t>(1, count) * 4) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_tasks, std::max<size_t>(1, all.size()) * sizeof(BatchTask)) == cudaSuccess;
+  ok = ok && cudaMalloc(&b->d_counters, 16) == cudaSuccess;
+  if (ok && count)
+    ok = cudaMemcpy(b->d_descs, descs, count * sizeof(fpa_batch_desc), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(b->d_order, order.data(), count * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+  if (ok && !all.empty())
+    ok = cudaMemcpy(b->d_tasks, all.data(), all.size() * sizeof(BatchTask), cudaMemcpyHostToDevice) == cudaSuccess;
+  ok = ok && cudaStreamCreateWithFlags(&b->side[0], cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && cudaStreamCreateWithFlags(&b->side[1], cudaStreamNonBlocking) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&b->ev_join[0], cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&b->ev_join[1], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) { fpa_batch_destroy(b); return fpa_device_error; }
+  *out = b;
+  return fpa_success;
+}
+
+static cudaError_t batch_enqueue(fpa_batch_t b, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *a_exps,
+                                 const uint32_t *a_limbs, const uint32_t *b_exps, const uint32_t *b_limbs,
+                                 cudaStream_t st) {
+  uint32_t *err;
+  int sms;
+  if (!gfpa_context(&sms, &err)) return cudaErrorUnknown;
+  cudaError_t e = cudaMemsetAsync(b->d_counters, 0, 16, st);
+  if (e != cudaSuccess) return e;
+  BatchArgs A;
+  A.descs = b->d_descs; A.order = b->d_order; A.err = err;
+  A.r_exps = r_exps; A.r_limbs = r_limbs; A.a_exps = a_exps; A.a_limbs = a_limbs;
+  A.b_exps = b_exps ? b_exps : a_exps; A.b_limbs = b_limbs ? b_limbs : a_limbs;
+  if ((e = cudaEventRecord(b->ev_fork, st)) != cudaSuccess) return e;
+  cudaStream_t streams[3] = {st, b->side[0], b->side[1]};
+  for (int c = 1; c < 3; c++)
+    if ((e = cudaStreamWaitEvent(streams[c], b->ev_fork, 0)) != cudaSuccess) return e;
+  for (int c = 0; c < 3; c++) {
+    if (!b->ntasks[c]) continue;
+    A.tasks = b->d_tasks + b->task_base[c];
+    A.ntasks = b->ntasks[c];
+    A.counter = b->d_counters + c;
+    A.warp_words = b->warp_words[c];
+    if ((e = launch(c, &A, b->grid[c], b->smem[c], streams[c])) != cudaSuccess) return e;
+  }
+  for (int c = 1; c < 3; c++) {
+    if ((e = cudaEventRecord(b->ev_join[c - 1], streams[c])) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, b->ev_join[c - 1], 0)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+extern "C" fpa_result fpa_batch_run(fpa_batch_t b, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *a_exps,
+                                    const uint32_t *a_limbs, const uint32_t *b_exps, const uint32_t *b_limbs,
+                                    void *stream) {
+  if (!b) return fpa_math_error;
+  if (b->count == 0) return fpa_success;
+  return batch_enqueue(b, r_exps, r_limbs, a_exps, a_limbs, b_exps, b_limbs, (cudaStream_t)stream) == cudaSuccess
+             ? fpa_success : fpa_device_error;
+}
+
+extern "C" fpa_result fpa_batch_capture(fpa_batch_t b, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *a_exps,
+                                        const uint32_t *a_limbs, const uint32_t *b_exps, const uint32_t *b_limbs) {
+  if (!b) return fpa_math_error;
+  if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+  if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+  if (b->count == 0) return fpa_success;
+  cudaStream_t cs;
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return fpa_device_error;
+  fpa_result res = fpa_device_error;
+  if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    cudaError_t e = batch_enqueue(b, r_exps, r_limbs, a_exps, a_limbs, b_exps, b_limbs, cs);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (e == cudaSuccess && e2 == cudaSuccess && g) {
+      b->graph = g;
+      if (cudaGraphInstantiate(&b->exec, g, 0) == cudaSuccess) res = fpa_success;
+    } else if (g) {
+      cudaGraphDestroy(g);
+    }
+  }
+  cudaStreamDestroy(cs);
+  return res;
+}
+
+extern "C" fpa_result fpa_batch_graph_launch(fpa_batch_t b, void *stream) {
+  if (!b) return fpa_math_error;
+  if (b->count == 0) return fpa_success;
+  if (!b->exec) return fpa_math_error;
+  return cudaGraphLaunch(b->exec, (cudaStream_t)stream) == cudaSuccess ? fpa_success : fpa_device_error;
+}
+
+extern "C" fpa_result fpa_batch_info(fpa_batch_t b, uint32_t *tasks_per_class, uint32_t *kernels) {
+  if (!b) return fpa_math_error;
+  uint32_t k = 0;
+  for (int c = 0; c < 3; c++) {
+    if (tasks_per_class) tasks_per_class[c] = b->ntasks[c];
+    k += b->ntasks[c] ? 1 : 0;
+  }
+  if (kernels) *kernels = k;
+  return fpa_success;
+}
+
+extern "C" fpa_result fpa_batch_destroy(fpa_batch_t b) {
+  if (!b) return fpa_success;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  for (int c = 0; c < 2; c++) {
+    if (b->ev_join[c]) cudaEventDestroy(b->ev_join[c]);
+    if (b->side[c]) cudaStreamDestroy(b->side[c]);
+  }
+  cudaFree(b->d_descs); cudaFree(b->d_order); cudaFree(b->d_tasks); cudaFree(b->d_counters);
+  delete b;
+  return fpa_success;
+}

@@ -1,0 +1,51 @@
+// fpa_batch.h -- internal interface of the batched and served forms.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+#include "../../include/fpa_gb300.h"
+
+// Per-process device context (SM count, device error word); false on CUDA failure.
+bool gfpa_context(int *sms, uint32_t **err);
+// Lane-group configuration for operation `op` on numbers of `n` limbs (autotuned table,
+// else the smallest default configuration that holds n).
+int gfpa_cfg_for_op(int op, uint32_t n);
+
+// One task = `count` operations of one (configuration, operation) pair, taken from the
+// sorted order array starting at `first`.
+struct BatchTask {
+  uint16_t key;      // cfg * 5 + op
+  uint16_t pad;
+  uint32_t first;
+  uint32_t count;
+};
+
+struct BatchArgs {
+  const fpa_batch_desc *descs;
+  const uint32_t *order;
+  const BatchTask *tasks;
+  uint32_t ntasks;
+  uint32_t *counter;          // next task of this class (device)
+  uint32_t warp_words;        // shared-memory words per warp
+  uint32_t *r_exps, *r_limbs;
+  const uint32_t *a_exps, *a_limbs, *b_exps, *b_limbs;
+  uint32_t *err;
+};
+
+// Register class of (configuration, operation): 0 = tiles <= 4 limbs for add/sub/mul,
+// 1 = 8-limb tiles and div/sqrt with tiles <= 8 limbs, 2 = 16-limb tiles.
+__host__ __device__ constexpr int gfpa_class_of(int cfg, int op) {
+  return (cfg == 6 || cfg == 8 || cfg == 9) ? 2 : ((cfg == 5 || cfg == 7 || op == 3 || op == 4) ? 1 : 0);
+}
+
+// threads per CTA of each class kernel
+static const int gfpa_class_threads[3] = {256, 128, 128};
+
+// Class kernels (fpa_batch_kernels.cu, one object per class).
+extern "C" {
+cudaError_t gfpa_batch_prepare0(size_t smem, int *blocks_per_sm);
+cudaError_t gfpa_batch_prepare1(size_t smem, int *blocks_per_sm);
+cudaError_t gfpa_batch_prepare2(size_t smem, int *blocks_per_sm);
+cudaError_t gfpa_batch_launch0(const BatchArgs *a, int grid, size_t smem, cudaStream_t st);
+cudaError_t gfpa_batch_launch1(const BatchArgs *a, int grid, size_t smem, cudaStream_t st);
+cudaError_t gfpa_batch_launch2(const BatchArgs *a, int grid, size_t smem, cudaStream_t st);
+}

@@ -319,22 +319,33 @@ __device__ __forceinline__ void columns_to_limbs(const uint32_t *lo, const uint3
   }
 }
 
-// Operands already staged in s.sa / s.sb for Mp = ceil(m/K) blocks.
 template <int G, int K>
-__device__ void grp_mulsq_staged(const Grp<G> &g, uint32_t *P, int m, const MulScratch<G, K> &s) {
+__device__ __forceinline__ void blocks_final_sum_inl(const Grp<G> g, uint32_t *P, int outlen, int Mp,
+                                                     const MulScratch<G, K> s);
+
+// Product P[0..lx+ly) of x (staged in s.sa, Ma = ceil(lx/K) blocks, zero padded) and y
+// (staged in s.sb at offset K, Mb = ceil(ly/K) <= Ma blocks, K zero limbs on each side).
+// Lane t < Ma owns column blocks t and t+Ma.  Block t holds min(t, Mb)+1 tiles and block
+// t+Ma holds max(0, Mb-t), so every lane runs exactly Mb+1 tile steps (for a square, Ma+1).
+// The first block's column sums are snapshotted at the lane's switch step (or after the
+// loop when there is no second block) and the second block is acc - snapshot.
+template <int G, int K>
+__device__ __forceinline__ void grp_mul_staged(const Grp<G> g, uint32_t *P, int lx, int ly, const MulScratch<G, K> s) {
   static_assert(K >= 2, "a column block must be at least 2 limbs wide");
-  const int Mp = (m + K - 1) / K;
+  const int Mp = (lx + K - 1) / K, Mb = (ly + K - 1) / K;
   const int t = (int)g.lane;
   const bool act = t < Mp;
+  const int n1 = (t < Mb ? t : Mb) + 1;          // tiles of block t
+  const int I0 = t > Mb ? t - Mb : 0;
   uint32_t lo[K], hi[K], tp[K];
 #pragma unroll
   for (int c = 0; c < K; c++) { lo[c] = 0; hi[c] = 0; tp[c] = 0; }
   if (act) {
-    for (int st = 0; st <= Mp; st++) {
-      const bool first = st <= t;
-      const int I = first ? st : st - 1;
+    for (int st = 0; st <= Mb; st++) {
+      const bool first = st < n1;
+      const int I = first ? I0 + st : t + Mp - Mb + (st - n1);
       const int cb = first ? t : t + Mp;
-      if (st == t + 1) {
+      if (st == n1) {
         uint32_t *sn = s.snap + t * 3 * K;
 #pragma unroll
         for (int c = 0; c < K; c++) { sn[c] = lo[c]; sn[K + c] = hi[c]; sn[2 * K + c] = tp[c]; }
@@ -368,7 +379,11 @@ __device__ void grp_mulsq_staged(const Grp<G> &g, uint32_t *P, int m, const MulS
   }
   // lane t: acc = blocks t + (t+Mp); snapshot = block t.  Emit both as K+2 limbs.
   if (act) {
-    const uint32_t *sn = s.snap + t * 3 * K;     // taken at step t+1 <= Mp
+    uint32_t *sn = s.snap + t * 3 * K;
+    if (n1 > Mb) {                               // no second block: snapshot = everything
+#pragma unroll
+      for (int c = 0; c < K; c++) { sn[c] = lo[c]; sn[K + c] = hi[c]; sn[2 * K + c] = tp[c]; }
+    }
     uint32_t L[K + 2];
     // second block = acc - snapshot (exact: each column sum < 2^96)
 #pragma unroll
@@ -389,7 +404,47 @@ __device__ void grp_mulsq_staged(const Grp<G> &g, uint32_t *P, int m, const MulS
     for (int j = 0; j < K + 2; j++) pp[j] = L[j];
   }
   g.sync();
-  // final sum: block cb = part[cb][0..K) + part[cb-1][K..K+2)
+  blocks_final_sum_inl<G, K>(g, P, lx + ly, Mp, s);
+}
+
+// square product of operands staged for m limbs each
+template <int G, int K>
+__device__ __forceinline__ void grp_mulsq_staged(const Grp<G> g, uint32_t *P, int m, const MulScratch<G, K> s) {
+  grp_mul_staged<G, K>(g, P, m, m, s);
+}
+
+// Out-of-line copy of the product for the operations that call it many times (div, sqrt):
+// one copy of the unrolled tile loop keeps their code inside the instruction cache.
+template <int G, int K>
+__device__ __noinline__ void grp_mul_call(const Grp<G> g, uint32_t *P, int lx, int ly, const MulScratch<G, K> s) {
+  grp_mul_staged<G, K>(g, P, lx, ly, s);
+}
+
+// P[0..lx+ly) = x[0..lx) * y[0..ly) for functor operands (lx, ly <= G*K, any order): the
+// longer one is staged as the block operand.
+template <int G, int K, class X, class Y>
+__device__ __forceinline__ void grp_mul(const Grp<G> &g, uint32_t *P, X x, int lx, Y y, int ly,
+                                        const MulScratch<G, K> &s) {
+  const bool swap = ly > lx;
+  const int la = swap ? ly : lx, lb = swap ? lx : ly;
+  const int Ma = (la + K - 1) / K, Mb = (lb + K - 1) / K;
+  for (int i = g.lane; i < Ma * K; i += G) s.sa[i] = (i < la) ? (swap ? y(i) : x(i)) : 0u;
+  for (int i = g.lane; i < Mb * K + 2 * K; i += G) {
+    const int j = i - K;
+    s.sb[i] = (j >= 0 && j < lb) ? (swap ? x(j) : y(j)) : 0u;
+  }
+  g.sync();
+  grp_mul_call<G, K>(g, P, la, lb, s);
+}
+
+// Sum of the per-block partials (K+2 limbs at block offsets K*cb) into P[0..outlen).
+// Lane t < Mp owns blocks t and t+Mp; carries between blocks by ballot lookahead.
+template <int G, int K>
+__device__ __forceinline__ void blocks_final_sum_inl(const Grp<G> g, uint32_t *P, int outlen, int Mp,
+                                                     const MulScratch<G, K> s) {
+  const int t = (int)g.lane;
+  const bool act = t < Mp;
+  // block cb = part[cb][0..K) + part[cb-1][K..K+2)
   uint32_t V0[K], V1[K];
   uint32_t g0 = 0, g1 = 0, p0 = 0, p1 = 0;
   if (act) {
@@ -429,7 +484,7 @@ __device__ void grp_mulsq_staged(const Grp<G> &g, uint32_t *P, int m, const MulS
         uint32_t v = V[j] + cin;
         cin = cin && (v == 0u);
         const int idx = K * cb + j;
-        if (idx < 2 * m) P[idx] = v;
+        if (idx < outlen) P[idx] = v;
       }
     }
   }
@@ -439,11 +494,7 @@ __device__ void grp_mulsq_staged(const Grp<G> &g, uint32_t *P, int m, const MulS
 // P[0..2m) = x[0..m) * y[0..m) with x, y functors (any storage); m <= G*K
 template <int G, int K, class X, class Y>
 __device__ __forceinline__ void grp_mulsq(const Grp<G> &g, uint32_t *P, X x, Y y, int m, const MulScratch<G, K> &s) {
-  const int Mp = (m + K - 1) / K, NK = Mp * K;
-  for (int i = g.lane; i < NK; i += G) s.sa[i] = (i < m) ? x(i) : 0u;
-  for (int i = g.lane; i < NK + 2 * K; i += G) { int j = i - K; s.sb[i] = (j >= 0 && j < m) ? y(j) : 0u; }
-  g.sync();
-  grp_mulsq_staged<G, K>(g, P, m, s);
+  grp_mul<G, K>(g, P, x, m, y, m, s);
 }
 
 }  // namespace gfpa

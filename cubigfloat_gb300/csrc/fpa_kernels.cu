@@ -32,6 +32,15 @@
 #elif GFPA_CFG == 6
 #define CFG_G 32
 #define CFG_K 16
+#elif GFPA_CFG == 7
+#define CFG_G 16
+#define CFG_K 8
+#elif GFPA_CFG == 8
+#define CFG_G 8
+#define CFG_K 16
+#elif GFPA_CFG == 9
+#define CFG_G 16
+#define CFG_K 16
 #else
 #error "unknown GFPA_CFG"
 #endif
@@ -43,19 +52,18 @@
 namespace gfpa {
 
 template <int OP, int G, int K>
-struct Words {
-  __host__ __device__ static constexpr int v() {
-    return MulScratch<G, K>::words() +
-           (OP == OP_ADD || OP == OP_SUB ? OpSpace<G, K>::addsub()
-            : OP == OP_MUL ? OpSpace<G, K>::mul()
-            : OP == OP_DIV ? OpSpace<G, K>::div() : OpSpace<G, K>::sqrt());
-  }
-  // keep each group's slice 16-byte aligned
-  __host__ __device__ static constexpr int aligned() { return (v() + 3) & ~3; }
+using Words = OpWords<OP, G, K>;
+
+// Register budgets (blocks of 128 threads per SM): 64 registers per thread for add/sub/mul
+// with tiles up to 4 limbs, 128 for 8-limb tiles and for div/sqrt (whose Newton loops keep
+// more state live), 255 for 16-limb tiles (a 16x16 tile holds 48 accumulators + 48 operands).
+template <int OP, int K>
+struct MinBlocks {
+  static constexpr int v = (K >= 16) ? 2 : ((OP == OP_DIV || OP == OP_SQRT || K >= 8) ? 4 : 8);
 };
 
 template <int OP, int G, int K>
-__global__ void __launch_bounds__(128) k_elementwise(ElementwiseArgs args) {
+__global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(ElementwiseArgs args) {
   extern __shared__ __align__(16) uint32_t smem[];
   Grp<G> g;
   const uint32_t gpc = blockDim.x / G, gi = threadIdx.x / G;

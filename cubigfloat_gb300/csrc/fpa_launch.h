@@ -17,12 +17,15 @@ struct ElementwiseArgs {
   uint32_t *err;
 };
 
-#define GFPA_NUM_CFGS 7
+#define GFPA_NUM_CFGS 10
+#define GFPA_NUM_DEFAULT_CFGS 7
 #define GFPA_MAX_LIMBS 512
 
-// limb capacity of each lane-group configuration (G lanes x K limbs per tile)
-static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32};
-static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16};
+// Lane-group configurations (G lanes x K limbs per tile, capacity G*K limbs).  0..6 are
+// the defaults in increasing capacity; 7..9 use fewer lanes with wider tiles so that two
+// or four operations share a warp, which the autotuner can choose (for div/sqrt).
+static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16};
+static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16};
 
 extern "C" {
 cudaError_t gfpa_launch_cfg0(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
@@ -32,11 +35,14 @@ cudaError_t gfpa_launch_cfg3(int op, const ElementwiseArgs *args, cudaStream_t s
 cudaError_t gfpa_launch_cfg4(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 cudaError_t gfpa_launch_cfg5(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 cudaError_t gfpa_launch_cfg6(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg7(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg8(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg9(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 }
 
-// smallest configuration whose capacity holds n limbs
+// smallest default configuration whose capacity holds n limbs
 static inline int gfpa_default_cfg(uint32_t n) {
-  for (int c = 0; c < GFPA_NUM_CFGS; c++)
+  for (int c = 0; c < GFPA_NUM_DEFAULT_CFGS; c++)
     if ((uint32_t)(gfpa_cfg_G[c] * gfpa_cfg_K[c]) >= n) return c;
   return -1;
 }
@@ -50,6 +56,9 @@ static inline cudaError_t gfpa_launch(int cfg, int op, const ElementwiseArgs *ar
     case 4: return gfpa_launch_cfg4(op, args, stream, sms);
     case 5: return gfpa_launch_cfg5(op, args, stream, sms);
     case 6: return gfpa_launch_cfg6(op, args, stream, sms);
+    case 7: return gfpa_launch_cfg7(op, args, stream, sms);
+    case 8: return gfpa_launch_cfg8(op, args, stream, sms);
+    case 9: return gfpa_launch_cfg9(op, args, stream, sms);
   }
   return cudaErrorInvalidValue;
 }

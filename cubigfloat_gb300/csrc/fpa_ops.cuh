@@ -26,6 +26,17 @@ struct OpSpace {
   __host__ __device__ static constexpr int words() { return MulScratch<G, K>::words() + max_all(); }
 };
 
+// Shared-memory words one group needs for operation OP (16-byte aligned slice size).
+template <int OP, int G, int K>
+struct OpWords {
+  __host__ __device__ static constexpr int v() {
+    return (OP == OP_ADD || OP == OP_SUB) ? OpSpace<G, K>::addsub()
+           : MulScratch<G, K>::words() + (OP == OP_MUL ? OpSpace<G, K>::mul()
+                                          : OP == OP_DIV ? OpSpace<G, K>::div() : OpSpace<G, K>::sqrt());
+  }
+  __host__ __device__ static constexpr int aligned() { return (v() + 3) & ~3; }
+};
+
 // Rounded mantissa + exponent for one instance, written by the group.
 template <int G, int PER>
 __device__ __forceinline__ void write_value(const Grp<G> &g, uint32_t *r_exp, uint32_t *r, int n,
@@ -71,7 +82,7 @@ __device__ void op_addsub(const Grp<G> &g, uint32_t *ws, int n, int mode, int is
   if (act == ACT_NEG_B) { copy_value<G>(g, r_exp, r, n, b_exp ^ 1u, b); return; }   // 0 - b = -b
   if (act != ACT_ADD && act != ACT_SUB) { write_class<G>(g, r_exp, act); return; }
 
-  uint32_t *sA = ws + MulScratch<G, K>::words(), *sB = sA + N, *X = sB + N;
+  uint32_t *sA = ws, *sB = sA + N, *X = sB + N;     // no product scratch needed
   for (int i = g.lane; i < n; i += G) { sA[i] = a[i]; sB[i] = b[i]; }
   g.sync();
   const uint32_t sa = a_exp & 1u, sb = (b_exp & 1u) ^ (uint32_t)is_sub;
@@ -165,13 +176,20 @@ struct SmallMul {
   }
 };
 
-// E[0..len) <- |E| (two's complement magnitude); returns the sign
-template <int G>
-__device__ __forceinline__ uint32_t grp_abs(const Grp<G> &g, uint32_t *E, int len) {
-  uint32_t neg = E[len - 1] >> 31;
-  if (neg) grp_sub<G>(g, E, Zero{}, Ptr{E, len}, len, 0u);
-  return neg;
-}
+// Newton residual magnitude read straight from a product T ~ 2^(32L):
+// |E| = |2^(32L) - T|, returned as limbs of |E| >> 32*off (i < len).  When T >= 2^(32L)
+// (neg) the low limbs of T are |E| itself; otherwise |E| = ~T + 1 and the +1 is dropped
+// (an error of one unit at 2^(32*off), far below the precision the step needs).
+struct ResidualMag {
+  const uint32_t *T; int off, L, len; uint32_t neg;
+  __device__ __forceinline__ uint32_t operator()(int i) const {
+    if (i < 0 || i >= len) return 0u;
+    const int idx = off + i;
+    if (idx >= L) return 0u;
+    const uint32_t v = T[idx];
+    return neg ? v : ~v;
+  }
+};
 
 // ---------------------------------------------------------------------------------------
 // div.  Reference: fpa_warp_div.h:127-201.
@@ -193,7 +211,7 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   uint32_t *sA = ws + MulScratch<G, K>::words(), *sB = sA + N;
   uint32_t *Y = sB + N, *Y2 = Y + (N + 4);
   uint32_t *T = Y2 + (N + 4), *P2 = T + (2 * N + 8);
-  uint32_t *E = P2 + (2 * N + 8), *Q = E + (N + 8), *R = Q + (N + 8);
+  uint32_t *Q = P2 + (2 * N + 8), *R = Q + (N + 8), *X = R + (N + 8);
   for (int i = g.lane; i < n; i += G) { sA[i] = a[i]; sB[i] = b[i]; }
   if (g.lane == 0) {
     uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)b[n - 1];   // level 1: floor((2^64-1)/B_top)
@@ -204,33 +222,21 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   const int nl = newton_levels(n, lv);
   for (int li = 1; li < nl; li++) {
     const int k = lv[li - 1], kp = lv[li];
-    const uint32_t ytop = Y[k];
     const uint32_t *Bk = sB + (n - kp);
-    // T = B_k' * Y_k  (2k' limbs suffice: k' + k + 1 <= 2k')
-    grp_mulsq<G, K>(g, T, Ptr{Bk, kp}, Ptr{Y, k}, kp, s);
-    grp_add<G>(g, T + k, Ptr{T + k, 2 * kp - k}, SmallMul{Bk, kp, ytop}, 2 * kp - k, 0u);
-    // E = (2^(32(k+k')) - T) mod 2^(32(k'+2))
-    const int le = kp + 2;
-    grp_sub<G>(g, E, Zero{}, Ptr{T, 2 * kp}, le, 0u);
-    if (k + kp < le && g.lane == 0) E[k + kp] += 1u;   // only k == 1: no carry can leave limb le-1
-    g.sync();
-    const uint32_t neg = grp_abs<G>(g, E, le);
+    // T = B_k' * Y_k   (k' x (k+1) limbs)
+    grp_mul<G, K>(g, T, Ptr{Bk, kp}, kp, Ptr{Y, k + 1}, k + 1, s);
     // M = (Y_k * (|E| >> 32(k-1))) >> 32(k+1)
-    const uint32_t *Et = E + (k - 1);
-    const int lt = le - (k - 1);
-    const int m2 = k > lt ? k : lt;
-    grp_mulsq<G, K>(g, P2, Ptr{Y, k}, Ptr{Et, lt}, m2, s);
-    if (g.lane == 0) { P2[2 * m2] = 0; P2[2 * m2 + 1] = 0; }
-    g.sync();
-    grp_add<G>(g, P2 + k, Ptr{P2 + k, 2 * m2 + 2 - k}, SmallMul{Et, lt, ytop}, 2 * m2 + 2 - k, 0u);
-    // Y_k' = Y_k * 2^(32(k'-k)) +- M
+    const int L = k + kp, lt = kp - k + 3;
+    const uint32_t neg = T[L] != 0u;
+    grp_mul<G, K>(g, P2, Ptr{Y, k + 1}, k + 1, ResidualMag{T, k - 1, L, lt, neg}, lt, s);
+    // Y_k' = Y_k * 2^(32(k'-k)) +- M   (E <= 0 means Y_k was too large)
     Shifted ysh{Y, k + 1, 32 * (kp - k)};
-    Ptr M{P2 + (k + 1), 2 * m2 + 1 - k};
+    Ptr M{P2 + (k + 1), lt};
     if (neg) grp_sub<G>(g, Y2, ysh, M, kp + 1, 0u);
     else grp_add<G>(g, Y2, ysh, M, kp + 1, 0u);
     uint32_t *tmp = Y; Y = Y2; Y2 = tmp;
   }
-  // Q = floor(A * Y / 2^(32n)),  n+1 limbs
+  // Q = floor(A * Y / 2^(32n)),  n+1 limbs;  Y = ytop*2^(32n) + Ylow
   const uint32_t ytop = Y[n];
   grp_mulsq<G, K>(g, T, Ptr{sA, n}, Ptr{Y, n}, n, s);
   if (g.lane == 0) { T[2 * n] = 0; T[2 * n + 1] = 0; }
@@ -260,11 +266,11 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   const int c2 = grp_cmp<G>(g, ShlBits{R, n + 2, 1}, Ptr{sB, n}, n + 2);
   const uint32_t rb = c2 >= 0 ? 1u : 0u;
   const uint32_t sticky = (!grp_is_zero<G>(g, Ptr{R, n + 2}, n + 2) && c2 != 0) ? 1u : 0u;
-  // X = 2Q + rb  (n+2 limbs), reuse E
-  grp_add<G>(g, E, ShlBits{Q, n + 1, 1}, Zero{}, n + 2, rb);
+  // X = 2Q + rb  (n+2 limbs)
+  grp_add<G>(g, X, ShlBits{Q, n + 1, 1}, Zero{}, n + 2, rb);
   const uint32_t sign = (a_exp ^ b_exp) & 1u;
   Rounded<G, K + 1> res;
-  grp_round<G, K + 1>(g, E, n + 2, n, sticky, mode, sign, res);
+  grp_round<G, K + 1>(g, X, n + 2, n, sticky, mode, sign, res);
   const long long e = (long long)(a_exp >> 1) - (long long)(b_exp >> 1) - 32LL * n - 1 + res.L + res.ovf;
   if ((long long)BIAS + e < 10) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
   if ((long long)BIAS + e >= 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
@@ -320,40 +326,21 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   const int nl = newton_levels(n, lv);
   for (int li = 1; li < nl; li++) {
     const int k = lv[li - 1], kp = lv[li];
-    const uint32_t ztop = Z[k];
-    // W = Z_k^2 = Zlow^2 + 2 ztop Zlow 2^(32k) + ztop^2 2^(64k)    (2k+2 limbs)
-    grp_mulsq<G, K>(g, W, Ptr{Z, k}, Ptr{Z, k}, k, s);
-    if (g.lane == 0) { W[2 * k] = 0; W[2 * k + 1] = 0; }
-    g.sync();
-    grp_add<G>(g, W + k, Ptr{W + k, k + 2}, SmallMul{Z, k, 2u * ztop}, k + 2, 0u);
-    if (ztop) {
-      const uint32_t zz = ztop * ztop;
-      grp_add<G>(g, W + 2 * k, Ptr{W + 2 * k, 2}, Ptr{&zz, 1}, 2, 0u);
-    }
-    // V = X_k' * W  mod 2^(32(k'+k+2)), W split at k' limbs
+    // W = Z_k^2  (Z_k has k+1 limbs)
+    grp_mulsq<G, K>(g, W, Ptr{Z, k + 1}, Ptr{Z, k + 1}, k + 1, s);
+    // V = X_k' * W = X*W[0..k') + (X*W[k'..2k+2)) << k'   (the second factor is short)
     const uint32_t *Xk = X2 + (2 * n - kp);
-    const int lw = 2 * k + 2;
-    grp_mulsq<G, K>(g, V1, Ptr{Xk, kp}, Ptr{W, kp < lw ? kp : lw}, kp, s);
-    grp_mulsq<G, K>(g, V2, Ptr{Xk, kp}, Ptr{W + kp, lw - kp}, kp, s);
-    const int lenV = kp + k + 2;
-    if (g.lane == 0) V1[2 * kp] = 0;
-    g.sync();
-    grp_add<G>(g, V1, Ptr{V1, 2 * kp + 1}, Shifted{V2, 2 * kp, 32 * kp}, lenV, 0u);
-    // E = (2^(32(k'+2k)) - V) mod 2^(32 lenV)
-    grp_sub<G>(g, E, Zero{}, Ptr{V1, lenV}, lenV, 0u);
-    if (kp + 2 * k < lenV && g.lane == 0) E[kp + 2 * k] += 1u;   // only k == 1 (top limb)
-    g.sync();
-    const uint32_t neg = grp_abs<G>(g, E, lenV);
-    // M = (Z_k * (|E| >> 32(2k-1))) >> (32(k+1) + 1)
-    const uint32_t *Et = E + (2 * k - 1);
-    const int lt = lenV - (2 * k - 1);
-    const int m2 = k > lt ? k : lt;
-    grp_mulsq<G, K>(g, P, Ptr{Z, k}, Ptr{Et, lt}, m2, s);
-    if (g.lane == 0) { P[2 * m2] = 0; P[2 * m2 + 1] = 0; }
-    g.sync();
-    grp_add<G>(g, P + k, Ptr{P + k, 2 * m2 + 2 - k}, SmallMul{Et, lt, ztop}, 2 * m2 + 2 - k, 0u);
+    const int ls = 2 * k + 2 - kp;
+    grp_mulsq<G, K>(g, V1, Ptr{Xk, kp}, Ptr{W, kp}, kp, s);
+    grp_mul<G, K>(g, V2, Ptr{Xk, kp}, kp, Ptr{W + kp, ls}, ls, s);
+    const int L = kp + 2 * k, lenV = L + 1;
+    grp_add<G>(g, V1, Ptr{V1, 2 * kp}, Shifted{V2, kp + ls, 32 * kp}, lenV, 0u);
+    // M = (Z_k * (|E| >> 32(2k-1))) >> (32(k+1) + 1),  E = 2^(32L) - V
+    const int lt = kp - k + 3;
+    const uint32_t neg = V1[L] != 0u;
+    grp_mul<G, K>(g, P, Ptr{Z, k + 1}, k + 1, ResidualMag{V1, 2 * k - 1, L, lt, neg}, lt, s);
     Shifted zsh{Z, k + 1, 32 * (kp - k)};
-    Shifted M{P, 2 * m2 + 2, -(32 * (k + 1) + 1)};
+    Shifted M{P, k + 1 + lt, -(32 * (k + 1) + 1)};
     if (neg) grp_sub<G>(g, Z2, zsh, M, kp + 1, 0u);
     else grp_add<G>(g, Z2, zsh, M, kp + 1, 0u);
     uint32_t *tmp = Z; Z = Z2; Z2 = tmp;

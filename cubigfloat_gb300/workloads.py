@@ -157,6 +157,71 @@ def config1(seed, count=65536, n=32):
     return a, b
 
 
+MIX_OPS = np.array([0, 1, 2, 3, 4])            # add, sub, mul, div, sqrt
+MIX_P = np.array([0.3, 0.2, 0.3, 0.1, 0.1])
+
+
+def mixed(seed, count, min_bits=256, max_bits=16384, mode=3, hard_frac=0.05, ops=None, limbs=None):
+    """Mixed batch (config 3): op drawn 30/20/30/10/10 from add/sub/mul/div/sqrt, precision
+    log-uniform in [min_bits, max_bits] rounded to whole limbs, operands as in config 2
+    (uniform mantissas, e in [-1000, 1000], positive sqrt arguments, `hard_frac`
+    near-halfway/near-exact cases, one construction per (op, limbs) pair).
+    Returns (descs, a_exps, a_limbs_flat, b_exps, b_limbs_flat, r_total) with descs in the
+    fpa_batch_desc layout."""
+    from cubigfloat_gb300 import BATCH_DESC
+    rng = np.random.default_rng(seed)
+    if ops is None:
+        ops = rng.choice(MIX_OPS, size=count, p=MIX_P).astype(np.uint8)
+    if limbs is None:
+        bits = 2.0 ** rng.uniform(np.log2(min_bits), np.log2(max_bits), size=count)
+        limbs = np.clip(np.rint(bits / 32), 1, 512).astype(np.uint16)
+    ops = np.asarray(ops, dtype=np.uint8)
+    limbs = np.asarray(limbs, dtype=np.uint16)
+    off = np.zeros(count + 1, dtype=np.uint64)
+    np.cumsum(limbs, out=off[1:])
+    total = int(off[-1])
+    a_limbs = rng.integers(0, 1 << 32, size=total, dtype=np.uint64).astype(np.uint32)
+    b_limbs = rng.integers(0, 1 << 32, size=total, dtype=np.uint64).astype(np.uint32)
+    tops = (off[1:] - 1).astype(np.int64)
+    a_limbs[tops] |= np.uint32(0x80000000)
+    b_limbs[tops] |= np.uint32(0x80000000)
+    ea = rng.integers(-1000, 1001, size=count)
+    eb = rng.integers(-1000, 1001, size=count)
+    sa = np.where(ops == 4, 0, rng.integers(0, 2, size=count))
+    a_exps = exp_word(ea, sa)
+    b_exps = exp_word(eb, rng.integers(0, 2, size=count))
+    nh = int(count * hard_frac)
+    if nh:
+        idx = rng.choice(count, size=nh, replace=False)
+        made = {}
+        for i in idx:
+            op, n = int(ops[i]), int(limbs[i])
+            if op == 4:
+                kind = "sqrt"
+            elif op == 3:
+                kind = "div"
+            else:
+                kind = "mul"
+            key = (kind, n)
+            if key not in made:
+                made[key] = {"mul": mul_near_half, "div": div_near_exact, "sqrt": sqrt_near_exact}[kind](rng, n)
+            A, B = made[key]
+            o = int(off[i])
+            a_limbs[o:o + n] = int_to_limbs(A, n)
+            if kind == "sqrt":
+                a_exps[i] = exp_word(2 * int(rng.integers(-500, 500)) + B, 0)
+            else:
+                b_limbs[o:o + n] = int_to_limbs(B, n)
+    descs = np.zeros(count, dtype=BATCH_DESC)
+    descs["op"] = ops
+    descs["mode"] = mode
+    descs["limbs"] = limbs
+    descs["r_off"] = off[:-1]
+    descs["a_off"] = off[:-1]
+    descs["b_off"] = off[:-1]
+    return descs, a_exps, a_limbs, b_exps, b_limbs, total
+
+
 def specials(n):
     """One operand of each class plus +-1.0 and +-0.75, for special-value tables."""
     one = np.zeros(n, dtype=np.uint32)

@@ -46,6 +46,45 @@ fpa_result fpa_gb300_config_shape(int cfg, uint32_t *lanes, uint32_t *tile_limbs
 fpa_result fpa_gb300_set_config(uint32_t limbs, int cfg);
 int fpa_gb300_get_config(uint32_t limbs);
 
+/* ---- batched form: many operations of mixed type and precision in one submission ----
+ *
+ * Each descriptor names one operation on numbers of `limbs` limbs (1..512); operand and
+ * result limbs live in caller-owned device pools at the given limb offsets, and exponent
+ * word i of the r/a/b exponent arrays belongs to descriptor i.  The plan sorts the
+ * operations into per-configuration tasks, picks each one's lane-group configuration from
+ * the autotuned table, and runs them with persistent kernels (one per register class,
+ * concurrent) that pull tasks from device work queues. */
+typedef struct {
+  uint8_t op;          /* fpa_op */
+  uint8_t mode;        /* fpa_rounding_mode */
+  uint16_t limbs;      /* precision / 32 */
+  uint32_t reserved;
+  uint64_t r_off, a_off, b_off;   /* limb offsets into the pools (b ignored for sqrt) */
+} fpa_batch_desc;
+
+typedef struct fpa_batch_s *fpa_batch_t;
+
+/* Build a plan for `count` host descriptors (copied to the device). */
+fpa_result fpa_batch_create(fpa_batch_t *batch, const fpa_batch_desc *descs, uint64_t count);
+/* Run the plan on `stream` (asynchronous). */
+fpa_result fpa_batch_run(fpa_batch_t batch, uint32_t *r_exps, uint32_t *r_limbs,
+                         const uint32_t *a_exps, const uint32_t *a_limbs,
+                         const uint32_t *b_exps, const uint32_t *b_limbs, void *stream);
+/* Capture one run (with these pointers) as a CUDA graph, then replay it with
+ * fpa_batch_graph_launch: one launch submits every task of the batch. */
+fpa_result fpa_batch_capture(fpa_batch_t batch, uint32_t *r_exps, uint32_t *r_limbs,
+                             const uint32_t *a_exps, const uint32_t *a_limbs,
+                             const uint32_t *b_exps, const uint32_t *b_limbs);
+fpa_result fpa_batch_graph_launch(fpa_batch_t batch, void *stream);
+/* number of tasks per register class (3 classes) and kernels per run, for inspection */
+fpa_result fpa_batch_info(fpa_batch_t batch, uint32_t *tasks_per_class, uint32_t *kernels);
+fpa_result fpa_batch_destroy(fpa_batch_t batch);
+
+/* Autotuned configuration table: the configuration used for `op` on numbers of `limbs`
+ * limbs (-1 = built-in default), settable per operation. */
+fpa_result fpa_gb300_set_op_config(fpa_op op, uint32_t limbs, int cfg);
+int fpa_gb300_get_op_config(fpa_op op, uint32_t limbs);
+
 /* Measured integer multiply-add throughput of the current GPU (mad.lo.u32 and mad.hi.u32
  * per second over all SMs): the roofline denominator for the multiply-bound operations. */
 fpa_result fpa_gb300_measure_imad_peak(double *mad_lo_per_s, double *mad_hi_per_s);

@@ -64,7 +64,7 @@ def test_argument_checks_without_device(lib):
     x = fpa.fpa_s()
     assert lib.fpa_init(P(x), 10, 1000) == fpa.fpa_invalid_precisions
     assert lib.fpa_init(P(x), 10, 16416) == fpa.fpa_invalid_precisions
-    assert lib.fpa_gb300_num_configs() == 7
+    assert lib.fpa_gb300_num_configs() == 10
     assert lib.fpa_gb300_get_config(128) == 4
     assert lib.fpa_gb300_get_config(513) == -1
 
