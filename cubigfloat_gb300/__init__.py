@@ -36,6 +36,12 @@ class FpaError(RuntimeError):
     pass
 
 
+class ServerConfig(ctypes.Structure):
+    """fpa_gb300.h: fpa_server_config"""
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
+                ("max_batch_ops", ctypes.c_uint32), ("batching", ctypes.c_int)]
+
+
 _lib = None
 
 
@@ -86,6 +92,16 @@ def lib():
         "fpa_batch_destroy": (i32, [vp]),
         "fpa_gb300_set_op_config": (i32, [i32, u32, i32]),
         "fpa_gb300_get_op_config": (i32, [i32, u32]),
+        "fpa_server_create": (i32, [ctypes.POINTER(vp), ctypes.POINTER(ServerConfig)]),
+        "fpa_server_submit": (ctypes.c_int64, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "fpa_server_wait": (i32, [vp, ctypes.c_int64, ctypes.c_int64]),
+        "fpa_server_job_times": (i32, [vp, ctypes.c_int64, ctypes.POINTER(u64), ctypes.POINTER(u64),
+                                       ctypes.POINTER(u64)]),
+        "fpa_server_release": (i32, [vp, ctypes.c_int64]),
+        "fpa_server_stats": (i32, [vp, ctypes.POINTER(u64)]),
+        "fpa_server_destroy": (i32, [vp]),
+        "fpa_gb300_dot": (i32, [u32, u64, u32, i32, vp, vp, vp, vp, vp, vp, vp]),
+        "fpa_gb300_newton_sqrt": (i32, [u32, u64, u32, i32, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -219,6 +235,20 @@ def device_errors():
     return lib().fpa_gb300_device_errors()
 
 
+def dot(precision, count, length, mode, r_exps, r_limbs, x_exps, x_limbs, y_exps, y_limbs, stream=0):
+    """fpa_gb300_dot on raw device addresses."""
+    v = ctypes.c_void_p
+    return lib().fpa_gb300_dot(precision, count, length, mode, v(r_exps), v(r_limbs), v(x_exps), v(x_limbs),
+                               v(y_exps), v(y_limbs), v(stream))
+
+
+def newton_sqrt(precision, count, iters, mode, y_exps, y_limbs, x_exps, x_limbs, stream=0):
+    """fpa_gb300_newton_sqrt on raw device addresses (y updated in place)."""
+    v = ctypes.c_void_p
+    return lib().fpa_gb300_newton_sqrt(precision, count, iters, mode, v(y_exps), v(y_limbs), v(x_exps),
+                                       v(x_limbs), v(stream))
+
+
 def configs():
     out = []
     for c in range(lib().fpa_gb300_num_configs()):
@@ -291,6 +321,66 @@ class Batch:
         if self.h:
             lib().fpa_batch_destroy(self.h)
             self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Server:
+    """fpa_server_t: request loop with continuous batching (batching=True) or plain
+    per-job launches (batching=False)."""
+
+    def __init__(self, hbm_budget_bytes=1 << 30, max_inflight=4, max_batch_ops=0, batching=True):
+        cfg = ServerConfig(hbm_budget_bytes, max_inflight, max_batch_ops, 1 if batching else 0)
+        self.h = ctypes.c_void_p()
+        rc = lib().fpa_server_create(ctypes.byref(self.h), ctypes.byref(cfg))
+        if rc != fpa_success:
+            raise FpaError(f"fpa_server_create -> {rc}")
+        self._keep = {}
+
+    def submit(self, precision, ops, modes, a_exps, a_limbs, b_exps=None, b_limbs=None):
+        """Submit one job; returns (job_id, (r_exps, r_limbs)) whose arrays are filled when
+        the job completes."""
+        ops = np.ascontiguousarray(ops, dtype=np.uint8)
+        count = ops.size
+        modes = np.ascontiguousarray(modes, dtype=np.uint8) if modes is not None else None
+        arrs = [np.ascontiguousarray(x, dtype=np.uint32) if x is not None else None
+                for x in (a_exps, a_limbs, b_exps, b_limbs)]
+        r_e = np.zeros(count, dtype=np.uint32)
+        r_l = np.zeros(count * (precision // 32), dtype=np.uint32)
+        p = lambda x: x.ctypes.data_as(ctypes.c_void_p) if x is not None else None
+        jid = lib().fpa_server_submit(self.h, precision, count, p(ops), p(modes), p(arrs[0]), p(arrs[1]),
+                                      p(arrs[2]), p(arrs[3]), p(r_e), p(r_l))
+        if jid <= 0:
+            raise FpaError(f"fpa_server_submit -> {-jid}")
+        self._keep[jid] = (ops, modes, arrs, r_e, r_l)
+        return jid, (r_e, r_l)
+
+    def wait(self, jid, timeout_ms=-1):
+        return lib().fpa_server_wait(self.h, jid, timeout_ms)
+
+    def times(self, jid):
+        a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        lib().fpa_server_job_times(self.h, jid, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value
+
+    def release(self, jid):
+        self._keep.pop(jid, None)
+        return lib().fpa_server_release(self.h, jid)
+
+    def stats(self):
+        s = (ctypes.c_uint64 * 6)()
+        lib().fpa_server_stats(self.h, s)
+        return dict(zip(["jobs", "ops", "batches", "peak_bytes", "failed", "budget_bytes"], list(s)))
+
+    def destroy(self):
+        if self.h:
+            lib().fpa_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+        self._keep.clear()
 
     def __del__(self):
         try:

@@ -67,30 +67,11 @@ cudaError_t launch(int c, const BatchArgs *a, int grid, size_t smem, cudaStream_
 
 }  // namespace
 
-struct fpa_batch_s {
-  uint64_t count = 0;
-  fpa_batch_desc *d_descs = nullptr;
-  uint32_t *d_order = nullptr;
-  BatchTask *d_tasks = nullptr;
-  uint32_t *d_counters = nullptr;     // one per class
-  uint32_t ntasks[3] = {0, 0, 0}, task_base[3] = {0, 0, 0};
-  uint32_t warp_words[3] = {0, 0, 0};
-  int grid[3] = {0, 0, 0};
-  size_t smem[3] = {0, 0, 0};
-  cudaStream_t side[2] = {nullptr, nullptr};
-  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-};
-
-extern "C" fpa_result fpa_batch_create(fpa_batch_t *out, const fpa_batch_desc *descs, uint64_t count) {
-  if (!out) return fpa_math_error;
-  *out = nullptr;
+fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan) {
   if (count > 0xFFFFFFFFull) return fpa_invalid_counts;
   if (count && !descs) return fpa_math_error;
-  int sms;
-  if (!gfpa_context(&sms, nullptr)) return fpa_device_error;
-  std::vector<uint32_t> order(count);
+  std::vector<uint32_t> &order = plan.order;
+  order.resize(count);
   std::vector<uint16_t> key(count);
   std::vector<uint8_t> cls(count);
   for (uint64_t i = 0; i < count; i++) {
@@ -129,30 +110,88 @@ extern "C" fpa_result fpa_batch_create(fpa_batch_t *out, const fpa_batch_desc *d
     }
     i = j;
   }
-  fpa_batch_s *b = new fpa_batch_s();
-  b->count = count;
-  std::vector<BatchTask> all;
+  plan.tasks.clear();
   for (int c = 0; c < 3; c++) {
     std::vector<size_t> idx(tasks[c].size());
     for (size_t q = 0; q < idx.size(); q++) idx[q] = q;
     std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return cost[c][x] > cost[c][y]; });
-    b->task_base[c] = (uint32_t)all.size();
-    b->ntasks[c] = (uint32_t)idx.size();
+    plan.task_base[c] = (uint32_t)plan.tasks.size();
+    plan.ntasks[c] = (uint32_t)idx.size();
     uint32_t ww = 0;
     for (size_t q : idx) {
-      all.push_back(tasks[c][q]);
+      plan.tasks.push_back(tasks[c][q]);
       ww = std::max<uint32_t>(ww, (uint32_t)warp_words_for(tasks[c][q].key / 5, tasks[c][q].key % 5));
     }
-    b->warp_words[c] = ww;
-    b->smem[c] = (size_t)(gfpa_class_threads[c] / 32) * ww * 4;
-    if (b->smem[c] > 227 * 1024) { fpa_batch_destroy(b); return fpa_device_error; }
-    if (b->ntasks[c]) {
+    plan.warp_words[c] = ww;
+    plan.smem[c] = (size_t)(gfpa_class_threads[c] / 32) * ww * 4;
+    plan.grid[c] = 0;
+    if (plan.smem[c] > 227 * 1024) return fpa_device_error;
+    if (plan.ntasks[c]) {
       int per = 0;
-      if (prepare(c, b->smem[c], &per) != cudaSuccess) { fpa_batch_destroy(b); return fpa_device_error; }
+      if (prepare(c, plan.smem[c], &per) != cudaSuccess) return fpa_device_error;
       if (per < 1) per = 1;
-      b->grid[c] = (int)std::min<uint64_t>((uint64_t)per * sms, b->ntasks[c]);
+      plan.grid[c] = (int)std::min<uint64_t>((uint64_t)per * sms, plan.ntasks[c]);
     }
   }
+  return fpa_success;
+}
+
+cudaError_t gfpa_batch_enqueue(const BatchPlan &plan, const fpa_batch_desc *d_descs, const uint32_t *d_order,
+                               const BatchTask *d_tasks, uint32_t *d_counters, uint32_t *r_exps, uint32_t *r_limbs,
+                               const uint32_t *a_exps, const uint32_t *a_limbs, const uint32_t *b_exps,
+                               const uint32_t *b_limbs, cudaStream_t st, const cudaStream_t side[2],
+                               cudaEvent_t fork, const cudaEvent_t join[2]) {
+  uint32_t *err;
+  int sms;
+  if (!gfpa_context(&sms, &err)) return cudaErrorUnknown;
+  cudaError_t e = cudaMemsetAsync(d_counters, 0, 16, st);
+  if (e != cudaSuccess) return e;
+  BatchArgs A;
+  A.descs = d_descs; A.order = d_order; A.err = err;
+  A.r_exps = r_exps; A.r_limbs = r_limbs; A.a_exps = a_exps; A.a_limbs = a_limbs;
+  A.b_exps = b_exps ? b_exps : a_exps; A.b_limbs = b_limbs ? b_limbs : a_limbs;
+  if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
+  const cudaStream_t streams[3] = {st, side[0], side[1]};
+  for (int c = 1; c < 3; c++)
+    if ((e = cudaStreamWaitEvent(streams[c], fork, 0)) != cudaSuccess) return e;
+  for (int c = 0; c < 3; c++) {
+    if (!plan.ntasks[c]) continue;
+    A.tasks = d_tasks + plan.task_base[c];
+    A.ntasks = plan.ntasks[c];
+    A.counter = d_counters + c;
+    A.warp_words = plan.warp_words[c];
+    if ((e = launch(c, &A, plan.grid[c], plan.smem[c], streams[c])) != cudaSuccess) return e;
+  }
+  for (int c = 1; c < 3; c++) {
+    if ((e = cudaEventRecord(join[c - 1], streams[c])) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, join[c - 1], 0)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+struct fpa_batch_s {
+  uint64_t count = 0;
+  BatchPlan plan;
+  fpa_batch_desc *d_descs = nullptr;
+  uint32_t *d_order = nullptr;
+  BatchTask *d_tasks = nullptr;
+  uint32_t *d_counters = nullptr;     // one per class
+  cudaStream_t side[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" fpa_result fpa_batch_create(fpa_batch_t *out, const fpa_batch_desc *descs, uint64_t count) {
+  if (!out) return fpa_math_error;
+  *out = nullptr;
+  int sms;
+  if (!gfpa_context(&sms, nullptr)) return fpa_device_error;
+  fpa_batch_s *b = new fpa_batch_s();
+  b->count = count;
+  fpa_result r = gfpa_batch_plan(descs, count, sms, b->plan);
+  if (r != fpa_success) { delete b; return r; }
+  const std::vector<BatchTask> &all = b->plan.tasks;
   bool ok = true;
   ok = ok && cudaMalloc(&b->d_descs, std::max<size_t>(1, count) * sizeof(fpa_batch_desc)) == cudaSuccess;
   ok = ok && cudaMalloc(&b->d_order, std::max<size_t>(1, count) * 4) == cudaSuccess;
@@ -160,7 +199,7 @@ extern "C" fpa_result fpa_batch_create(fpa_batch_t *out, const fpa_batch_desc *d
   ok = ok && cudaMalloc(&b->d_counters, 16) == cudaSuccess;
   if (ok && count)
     ok = cudaMemcpy(b->d_descs, descs, count * sizeof(fpa_batch_desc), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(b->d_order, order.data(), count * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+         cudaMemcpy(b->d_order, b->plan.order.data(), count * 4, cudaMemcpyHostToDevice) == cudaSuccess;
   if (ok && !all.empty())
     ok = cudaMemcpy(b->d_tasks, all.data(), all.size() * sizeof(BatchTask), cudaMemcpyHostToDevice) == cudaSuccess;
   ok = ok && cudaStreamCreateWithFlags(&b->side[0], cudaStreamNonBlocking) == cudaSuccess;
@@ -176,32 +215,8 @@ extern "C" fpa_result fpa_batch_create(fpa_batch_t *out, const fpa_batch_desc *d
 static cudaError_t batch_enqueue(fpa_batch_t b, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *a_exps,
                                  const uint32_t *a_limbs, const uint32_t *b_exps, const uint32_t *b_limbs,
                                  cudaStream_t st) {
-  uint32_t *err;
-  int sms;
-  if (!gfpa_context(&sms, &err)) return cudaErrorUnknown;
-  cudaError_t e = cudaMemsetAsync(b->d_counters, 0, 16, st);
-  if (e != cudaSuccess) return e;
-  BatchArgs A;
-  A.descs = b->d_descs; A.order = b->d_order; A.err = err;
-  A.r_exps = r_exps; A.r_limbs = r_limbs; A.a_exps = a_exps; A.a_limbs = a_limbs;
-  A.b_exps = b_exps ? b_exps : a_exps; A.b_limbs = b_limbs ? b_limbs : a_limbs;
-  if ((e = cudaEventRecord(b->ev_fork, st)) != cudaSuccess) return e;
-  cudaStream_t streams[3] = {st, b->side[0], b->side[1]};
-  for (int c = 1; c < 3; c++)
-    if ((e = cudaStreamWaitEvent(streams[c], b->ev_fork, 0)) != cudaSuccess) return e;
-  for (int c = 0; c < 3; c++) {
-    if (!b->ntasks[c]) continue;
-    A.tasks = b->d_tasks + b->task_base[c];
-    A.ntasks = b->ntasks[c];
-    A.counter = b->d_counters + c;
-    A.warp_words = b->warp_words[c];
-    if ((e = launch(c, &A, b->grid[c], b->smem[c], streams[c])) != cudaSuccess) return e;
-  }
-  for (int c = 1; c < 3; c++) {
-    if ((e = cudaEventRecord(b->ev_join[c - 1], streams[c])) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(st, b->ev_join[c - 1], 0)) != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  return gfpa_batch_enqueue(b->plan, b->d_descs, b->d_order, b->d_tasks, b->d_counters, r_exps, r_limbs, a_exps,
+                            a_limbs, b_exps, b_limbs, st, b->side, b->ev_fork, b->ev_join);
 }
 
 extern "C" fpa_result fpa_batch_run(fpa_batch_t b, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *a_exps,
@@ -248,8 +263,8 @@ extern "C" fpa_result fpa_batch_info(fpa_batch_t b, uint32_t *tasks_per_class, u
   if (!b) return fpa_math_error;
   uint32_t k = 0;
   for (int c = 0; c < 3; c++) {
-    if (tasks_per_class) tasks_per_class[c] = b->ntasks[c];
-    k += b->ntasks[c] ? 1 : 0;
+    if (tasks_per_class) tasks_per_class[c] = b->plan.ntasks[c];
+    k += b->plan.ntasks[c] ? 1 : 0;
   }
   if (kernels) *kernels = k;
   return fpa_success;

@@ -40,6 +40,27 @@ __host__ __device__ constexpr int gfpa_class_of(int cfg, int op) {
 // threads per CTA of each class kernel
 static const int gfpa_class_threads[3] = {256, 128, 128};
 
+// Host-side plan of a batch: descriptor order, tasks (concatenated class by class) and the
+// launch shape of each class kernel.
+#include <vector>
+struct BatchPlan {
+  std::vector<uint32_t> order;
+  std::vector<BatchTask> tasks;
+  uint32_t ntasks[3] = {0, 0, 0}, task_base[3] = {0, 0, 0}, warp_words[3] = {0, 0, 0};
+  size_t smem[3] = {0, 0, 0};
+  int grid[3] = {0, 0, 0};
+};
+// Plan `count` descriptors; fpa_success or the validation error.
+fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan);
+// Enqueue one run of a plan whose descriptors, order and tasks are already in device memory.
+// Class 0 runs on `st`, classes 1 and 2 on `side[0]`, `side[1]` (forked from and joined back
+// into `st` with the given events).
+cudaError_t gfpa_batch_enqueue(const BatchPlan &plan, const fpa_batch_desc *d_descs, const uint32_t *d_order,
+                               const BatchTask *d_tasks, uint32_t *d_counters, uint32_t *r_exps, uint32_t *r_limbs,
+                               const uint32_t *a_exps, const uint32_t *a_limbs, const uint32_t *b_exps,
+                               const uint32_t *b_limbs, cudaStream_t st, const cudaStream_t side[2],
+                               cudaEvent_t fork, const cudaEvent_t join[2]);
+
 // Class kernels (fpa_batch_kernels.cu, one object per class).
 extern "C" {
 cudaError_t gfpa_batch_prepare0(size_t smem, int *blocks_per_sm);

@@ -57,9 +57,13 @@ using Words = OpWords<OP, G, K>;
 // Register budgets (blocks of 128 threads per SM): 64 registers per thread for add/sub/mul
 // with tiles up to 4 limbs, 128 for 8-limb tiles and for div/sqrt (whose Newton loops keep
 // more state live), 255 for 16-limb tiles (a 16x16 tile holds 48 accumulators + 48 operands).
+#ifndef GFPA_NEWTON_MINBLOCKS
+#define GFPA_NEWTON_MINBLOCKS 4
+#endif
 template <int OP, int K>
 struct MinBlocks {
-  static constexpr int v = (K >= 16) ? 2 : ((OP == OP_DIV || OP == OP_SQRT || K >= 8) ? 4 : 8);
+  static constexpr int v = (K >= 16) ? 2
+                           : ((OP == OP_DIV || OP == OP_SQRT) ? (K >= 8 ? 4 : GFPA_NEWTON_MINBLOCKS) : (K >= 8 ? 4 : 8));
 };
 
 template <int OP, int G, int K>

@@ -222,6 +222,31 @@ def mixed(seed, count, min_bits=256, max_bits=16384, mode=3, hard_frac=0.05, ops
     return descs, a_exps, a_limbs, b_exps, b_limbs, total
 
 
+SERVED_PRECISIONS = (512, 1024, 4096, 16384)
+
+
+def served_job(rng, precision=None, size=None, max_ops=4096):
+    """One served request (config 5): a precision from {512, 1024, 4096, 16384} bits, a size
+    log-uniform in [1, max_ops], ops drawn 30/20/30/10/10, operands as in config 2 without
+    the hard cases.  Returns (precision, ops, modes, a_exps, a_limbs, b_exps, b_limbs)."""
+    if precision is None:
+        precision = int(rng.choice(SERVED_PRECISIONS))
+    if size is None:
+        size = int(np.clip(np.rint(2.0 ** rng.uniform(0, np.log2(max_ops))), 1, max_ops))
+    n = precision // 32
+    ops = rng.choice(MIX_OPS, size=size, p=MIX_P).astype(np.uint8)
+    ae, al = uniform(rng, size, n, -1000, 1000)
+    be, bl = uniform(rng, size, n, -1000, 1000)
+    ae = np.where(ops == 4, ae & ~np.uint32(1), ae).astype(np.uint32)
+    modes = np.full(size, 3, np.uint8)
+    return precision, ops, modes, ae, al.reshape(-1), be, bl.reshape(-1)
+
+
+def poisson_arrivals(rng, njobs, rate_per_s):
+    """Arrival times (seconds from start) of a Poisson process."""
+    return np.cumsum(rng.exponential(1.0 / rate_per_s, size=njobs))
+
+
 def specials(n):
     """One operand of each class plus +-1.0 and +-0.75, for special-value tables."""
     one = np.zeros(n, dtype=np.uint32)

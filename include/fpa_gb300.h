@@ -80,6 +80,59 @@ fpa_result fpa_batch_graph_launch(fpa_batch_t batch, void *stream);
 fpa_result fpa_batch_info(fpa_batch_t batch, uint32_t *tasks_per_class, uint32_t *kernels);
 fpa_result fpa_batch_destroy(fpa_batch_t batch);
 
+/* ---- fused chains (intermediates stay in on-chip shared memory, one launch) ----------
+ *
+ * Dot products: r_d = RN(... RN(RN(x_{d,0} y_{d,0}) + RN(x_{d,1} y_{d,1})) ...), every
+ * product and every addition rounded in `mode`, accumulated in order from zero.  Element i
+ * of dot d is number d*len + i of the x and y arrays (device). */
+fpa_result fpa_gb300_dot(uint32_t precision, uint64_t count, uint32_t len, fpa_rounding_mode mode,
+                         uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *x_exps, const uint32_t *x_limbs,
+                         const uint32_t *y_exps, const uint32_t *y_limbs, void *stream);
+/* Newton square root: `iters` times y <- RN(RN(y + RN(x / y)) * 0.5), y updated in place
+ * (y holds the starting values on entry). */
+fpa_result fpa_gb300_newton_sqrt(uint32_t precision, uint64_t count, uint32_t iters, fpa_rounding_mode mode,
+                                 uint32_t *y_exps, uint32_t *y_limbs, const uint32_t *x_exps,
+                                 const uint32_t *x_limbs, void *stream);
+
+/* ---- served form: a request loop with continuous batching ----------------------------
+ *
+ * Jobs (one precision, `count` operations of mixed type) are submitted from any thread;
+ * a server thread keeps up to `max_inflight` batches on the GPU, each in a slot whose
+ * device arena is `hbm_budget_bytes / max_inflight` (allocated once, at creation).  When a
+ * slot frees, pending jobs are admitted in arrival order while they fit its arena, so jobs
+ * arriving while others run join the next batch and overlap with the batches in flight.
+ * `batching = 0` serves each job alone with plain per-operation-type launches (the
+ * comparison point).  Host arrays passed to submit must stay valid until the job is done;
+ * results are written to r_exps / r_limbs (host) on completion. */
+typedef struct {
+  uint64_t hbm_budget_bytes;
+  uint32_t max_inflight;
+  uint32_t max_batch_ops;   /* 0 = no limit beyond the arena */
+  int batching;             /* 1 = continuous batching, 0 = plain per-job launches */
+} fpa_server_config;
+
+typedef struct fpa_server_s *fpa_server_t;
+
+fpa_result fpa_server_create(fpa_server_t *server, const fpa_server_config *config);
+/* Returns a job id > 0, or minus an fpa_result code (e.g. -fpa_invalid_counts when the job
+ * is larger than one slot's share of the budget). modes may be NULL (ties to even);
+ * b_exps/b_limbs may be NULL when every operation is a sqrt. */
+int64_t fpa_server_submit(fpa_server_t server, uint32_t precision, uint32_t count, const uint8_t *ops,
+                          const uint8_t *modes, const uint32_t *a_exps, const uint32_t *a_limbs,
+                          const uint32_t *b_exps, const uint32_t *b_limbs, uint32_t *r_exps, uint32_t *r_limbs);
+/* Wait for a job (timeout_ms < 0: no limit); fpa_success once its results are written. */
+fpa_result fpa_server_wait(fpa_server_t server, int64_t job, int64_t timeout_ms);
+/* Nanoseconds since server creation at submission, admission to a batch, completion. */
+fpa_result fpa_server_job_times(fpa_server_t server, int64_t job, uint64_t *t_submit, uint64_t *t_admit,
+                                uint64_t *t_done);
+/* Forget a finished job. */
+fpa_result fpa_server_release(fpa_server_t server, int64_t job);
+/* stats[6]: jobs done, operations done, batches launched, peak resident bytes, failed jobs,
+ * budget bytes. */
+fpa_result fpa_server_stats(fpa_server_t server, uint64_t *stats);
+/* Finish pending work and free everything. */
+fpa_result fpa_server_destroy(fpa_server_t server);
+
 /* Autotuned configuration table: the configuration used for `op` on numbers of `limbs`
  * limbs (-1 = built-in default), settable per operation. */
 fpa_result fpa_gb300_set_op_config(fpa_op op, uint32_t limbs, int cfg);
