@@ -45,6 +45,7 @@ def _units():
     units.append(("fpa_probe.cu", [], "fpa_probe.o"))
     units.append(("fpa_batch.cu", [], "fpa_batch.o"))
     units.append(("fpa_chain.cu", [], "fpa_chain.o"))
+    units.append(("fpa_batch_noalloc.cu", [], "fpa_batch_noalloc.o"))
     for c in range(3):
         units.append(("fpa_batch_kernels.cu", [f"-DGFPA_BATCH_CLASS={c}"], f"fpa_batch_kernels_cls{c}.o"))
     units.append(("fpa_serve.cu", [], "fpa_serve.o"))

@@ -67,6 +67,13 @@ cudaError_t launch(int c, const BatchArgs *a, int grid, size_t smem, cudaStream_
 
 }  // namespace
 
+int gfpa_batch_warp_words(int cfg, int op) { return warp_words_for(cfg, op); }
+double gfpa_batch_op_weight(int op, int n) { return op_weight(op, n); }
+cudaError_t gfpa_batch_prepare_class(int c, size_t smem, int *per_sm) { return prepare(c, smem, per_sm); }
+cudaError_t gfpa_batch_launch_class(int c, const BatchArgs *a, int grid, size_t smem, cudaStream_t st) {
+  return launch(c, a, grid, smem, st);
+}
+
 fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan) {
   if (count > 0xFFFFFFFFull) return fpa_invalid_counts;
   if (count && !descs) return fpa_math_error;

@@ -61,6 +61,12 @@ cudaError_t gfpa_batch_enqueue(const BatchPlan &plan, const fpa_batch_desc *d_de
                                const uint32_t *b_limbs, cudaStream_t st, const cudaStream_t side[2],
                                cudaEvent_t fork, const cudaEvent_t join[2]);
 
+// Planner helpers shared with other entry points of the batched form.
+int gfpa_batch_warp_words(int cfg, int op);          // shared-memory words per warp
+double gfpa_batch_op_weight(int op, int n);           // relative cost of one operation
+cudaError_t gfpa_batch_prepare_class(int c, size_t smem, int *blocks_per_sm);
+cudaError_t gfpa_batch_launch_class(int c, const BatchArgs *a, int grid, size_t smem, cudaStream_t st);
+
 // Class kernels (fpa_batch_kernels.cu, one object per class).
 extern "C" {
 cudaError_t gfpa_batch_prepare0(size_t smem, int *blocks_per_sm);

@@ -133,6 +133,25 @@ fpa_result fpa_server_stats(fpa_server_t server, uint64_t *stats);
 /* Finish pending work and free everything. */
 fpa_result fpa_server_destroy(fpa_server_t server);
 
+/* Batched run without any memory allocation.  No counterpart in the reference.
+ *
+ * For callers that may not allocate GPU memory where they compute (while a stream is being
+ * captured into a graph, inside a serving loop that must never wait on the allocator, or
+ * in a host application that fixes this library's memory footprint up front): inputs and
+ * outputs are the caller's device arrays, and the batch's working memory is one fixed
+ * device array sized for FPA_NOALLOC_MAX_OPS operations, which every GPU that loads the
+ * library holds until the process exits.  More operations than that: fpa_invalid_counts.
+ * The first call on each device looks up that array's address and must come before any
+ * stream capture.  All calls share the array (it keeps the last call's contents; each call
+ * clears its counters and error word itself), so calls must not overlap on the GPU.  The
+ * host descriptors are read during the call.  Error bits of the bounded correction loops
+ * are read with fpa_batch_noalloc_errors (which synchronizes `stream`). */
+#define FPA_NOALLOC_MAX_OPS 4096
+fpa_result fpa_batch_run_noalloc(const fpa_batch_desc *descs, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs,
+                                 const uint32_t *a_exps, const uint32_t *a_limbs,
+                                 const uint32_t *b_exps, const uint32_t *b_limbs, void *stream);
+uint32_t fpa_batch_noalloc_errors(void *stream);
+
 /* Autotuned configuration table: the configuration used for `op` on numbers of `limbs`
  * limbs (-1 = built-in default), settable per operation. */
 fpa_result fpa_gb300_set_op_config(fpa_op op, uint32_t limbs, int cfg);
