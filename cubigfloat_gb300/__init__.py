@@ -79,7 +79,7 @@ def lib():
         "fpa_copy_array_to_host_async": (i32, [P, vp, vp, vp]),
         "fpa_gb300_device_errors": (u32, []),
         "fpa_gb300_num_configs": (i32, []),
-        "fpa_gb300_config_shape": (i32, [i32, ctypes.POINTER(u32), ctypes.POINTER(u32)]),
+        "fpa_gb300_config_shape": (i32, [i32, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32)]),
         "fpa_gb300_set_config": (i32, [u32, i32]),
         "fpa_gb300_get_config": (i32, [u32]),
         "fpa_gb300_version": (ctypes.c_char_p, []),
@@ -102,6 +102,8 @@ def lib():
         "fpa_server_destroy": (i32, [vp]),
         "fpa_gb300_dot": (i32, [u32, u64, u32, i32, vp, vp, vp, vp, vp, vp, vp]),
         "fpa_gb300_newton_sqrt": (i32, [u32, u64, u32, i32, vp, vp, vp, vp, vp]),
+        "fpa_gb300_autotune": (i32, [i32, u32, u32, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_double)]),
+        "fpa_gb300_load_tuning": (i32, [ctypes.c_char_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -252,9 +254,9 @@ def newton_sqrt(precision, count, iters, mode, y_exps, y_limbs, x_exps, x_limbs,
 def configs():
     out = []
     for c in range(lib().fpa_gb300_num_configs()):
-        g, k = ctypes.c_uint32(), ctypes.c_uint32()
-        lib().fpa_gb300_config_shape(c, ctypes.byref(g), ctypes.byref(k))
-        out.append((g.value, k.value))
+        g, k, r = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        lib().fpa_gb300_config_shape(c, ctypes.byref(g), ctypes.byref(k), ctypes.byref(r))
+        out.append((g.value, k.value, r.value))
     return out
 
 

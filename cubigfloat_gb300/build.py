@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfpa_gb300.so")
-NUM_CFGS = 10
+NUM_CFGS = 16
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
@@ -45,6 +45,7 @@ def _units():
     units.append(("fpa_probe.cu", [], "fpa_probe.o"))
     units.append(("fpa_batch.cu", [], "fpa_batch.o"))
     units.append(("fpa_chain.cu", [], "fpa_chain.o"))
+    units.append(("fpa_tune.cu", [], "fpa_tune.o"))
     units.append(("fpa_batch_noalloc.cu", [], "fpa_batch_noalloc.o"))
     for c in range(3):
         units.append(("fpa_batch_kernels.cu", [f"-DGFPA_BATCH_CLASS={c}"], f"fpa_batch_kernels_cls{c}.o"))

@@ -21,8 +21,9 @@ struct State {
   int device = -1;
   int sms = 0;
   uint32_t *err = nullptr;                // device error word
-  int8_t cfg_override[5][GFPA_MAX_LIMBS + 1];   // per operation and limb count, -1 = default
-  State() { memset(cfg_override, -1, sizeof cfg_override); }
+  // per operation and limb count: configuration + 1, 0 = default.  Zero-initialised (no
+  // constructor), so the table is ready before any static initialiser of another file runs.
+  int8_t cfg_override[5][GFPA_MAX_LIMBS + 1];
 };
 State g_state;
 
@@ -39,15 +40,15 @@ bool gfpa_context(int *sms, uint32_t **err) {
 }
 
 static bool cfg_fits(int c, uint32_t n) {
-  const uint32_t cap = (uint32_t)(gfpa_cfg_G[c] * gfpa_cfg_K[c]);
+  const uint32_t cap = (uint32_t)gfpa_cfg_capacity(c);
   return cap >= n && cap >= 4;
 }
 
 int gfpa_cfg_for_op(int op, uint32_t n) {
   if (op < 0 || op > 4 || n == 0 || n > GFPA_MAX_LIMBS) return -1;
-  int c = g_state.cfg_override[op][n];
+  const int c = g_state.cfg_override[op][n] - 1;
   if (c >= 0 && cfg_fits(c, n)) return c;
-  return gfpa_default_cfg(n);
+  return gfpa_default_cfg(n < 4 ? 4 : n);
 }
 
 namespace {
@@ -266,10 +267,11 @@ uint32_t fpa_gb300_device_errors(void) {
 
 int fpa_gb300_num_configs(void) { return GFPA_NUM_CFGS; }
 
-fpa_result fpa_gb300_config_shape(int cfg, uint32_t *lanes, uint32_t *tile_limbs) {
+fpa_result fpa_gb300_config_shape(int cfg, uint32_t *lanes, uint32_t *tile_limbs, uint32_t *pairs) {
   if (cfg < 0 || cfg >= GFPA_NUM_CFGS) return fpa_math_error;
   if (lanes) *lanes = (uint32_t)gfpa_cfg_G[cfg];
   if (tile_limbs) *tile_limbs = (uint32_t)gfpa_cfg_K[cfg];
+  if (pairs) *pairs = (uint32_t)gfpa_cfg_R[cfg];
   return fpa_success;
 }
 
@@ -279,7 +281,7 @@ fpa_result fpa_gb300_set_op_config(fpa_op op, uint32_t limbs, int cfg) {
   if (cfg < -1 || cfg >= GFPA_NUM_CFGS) return fpa_math_error;
   if (cfg >= 0 && !cfg_fits(cfg, limbs)) return fpa_invalid_precisions;
   std::lock_guard<std::mutex> lk(g_state.mu);
-  g_state.cfg_override[(int)op][limbs] = (int8_t)cfg;
+  g_state.cfg_override[(int)op][limbs] = (int8_t)(cfg + 1);
   return fpa_success;
 }
 

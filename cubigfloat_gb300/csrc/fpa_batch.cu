@@ -23,17 +23,19 @@ namespace {
 
 // shared-memory words one warp needs for (configuration, operation)
 int warp_words_for(int cfg, int op) {
-#define GFPA_W(CFG, GG, KK)                                                                   \
+#define GFPA_W(CFG, GG, KK, RR)                                                               \
   if (cfg == CFG) {                                                                          \
     switch (op) {                                                                            \
-      case OP_ADD: case OP_SUB: return (32 / GG) * OpWords<OP_ADD, GG, KK>::aligned();         \
-      case OP_MUL: return (32 / GG) * OpWords<OP_MUL, GG, KK>::aligned();                       \
-      case OP_DIV: return (32 / GG) * OpWords<OP_DIV, GG, KK>::aligned();                       \
-      default: return (32 / GG) * OpWords<OP_SQRT, GG, KK>::aligned();                          \
+      case OP_ADD: case OP_SUB: return (32 / GG) * OpWords<OP_ADD, GG, KK, RR>::aligned();     \
+      case OP_MUL: return (32 / GG) * OpWords<OP_MUL, GG, KK, RR>::aligned();                   \
+      case OP_DIV: return (32 / GG) * OpWords<OP_DIV, GG, KK, RR>::aligned();                   \
+      default: return (32 / GG) * OpWords<OP_SQRT, GG, KK, RR>::aligned();                      \
     }                                                                                        \
   }
-  GFPA_W(0, 4, 2) GFPA_W(1, 8, 2) GFPA_W(2, 8, 4) GFPA_W(3, 16, 4) GFPA_W(4, 32, 4) GFPA_W(5, 32, 8) GFPA_W(6, 32, 16)
-  GFPA_W(7, 16, 8) GFPA_W(8, 8, 16) GFPA_W(9, 16, 16)
+  GFPA_W(0, 4, 2, 1) GFPA_W(1, 8, 2, 1) GFPA_W(2, 8, 4, 1) GFPA_W(3, 16, 4, 1) GFPA_W(4, 32, 4, 1)
+  GFPA_W(5, 32, 8, 1) GFPA_W(6, 32, 16, 1) GFPA_W(7, 16, 8, 1) GFPA_W(8, 8, 16, 1) GFPA_W(9, 16, 16, 1)
+  GFPA_W(10, 8, 4, 2) GFPA_W(11, 8, 4, 4) GFPA_W(12, 16, 4, 2) GFPA_W(13, 8, 8, 4) GFPA_W(14, 16, 8, 2)
+  GFPA_W(15, 4, 4, 8)
 #undef GFPA_W
   return 0;
 }
@@ -85,8 +87,12 @@ fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms,
     const fpa_batch_desc &d = descs[i];
     if (d.op > 4 || d.mode > 4) return fpa_math_error;
     if (d.limbs == 0 || d.limbs > GFPA_MAX_LIMBS) return fpa_invalid_precisions;
-    const int cfg = gfpa_cfg_for_op(d.op, d.limbs);
+    int cfg = gfpa_cfg_for_op(d.op, d.limbs);
     if (cfg < 0) return fpa_invalid_precisions;
+    // a chosen configuration whose warps need more shared memory than one CTA of its class
+    // can hold gives way to the default one
+    if ((size_t)(gfpa_class_threads[gfpa_class_of(cfg, d.op)] / 32) * warp_words_for(cfg, d.op) * 4 > 227 * 1024)
+      cfg = gfpa_default_cfg(d.limbs < 4 ? 4 : d.limbs);
     key[i] = (uint16_t)(cfg * 5 + d.op);
     cls[i] = (uint8_t)gfpa_class_of(cfg, d.op);
     order[i] = (uint32_t)i;

@@ -31,10 +31,15 @@ struct BatchArgs {
   uint32_t *err;
 };
 
+// Tile width K of configuration cfg (the table in fpa_launch.h, usable in device code).
+__host__ __device__ constexpr int gfpa_cfg_tile(int cfg) {
+  return (cfg == 6 || cfg == 8 || cfg == 9) ? 16 : ((cfg == 5 || cfg == 7 || cfg == 13 || cfg == 14) ? 8 : (cfg <= 1 ? 2 : 4));
+}
+
 // Register class of (configuration, operation): 0 = tiles <= 4 limbs for add/sub/mul,
 // 1 = 8-limb tiles and div/sqrt with tiles <= 8 limbs, 2 = 16-limb tiles.
 __host__ __device__ constexpr int gfpa_class_of(int cfg, int op) {
-  return (cfg == 6 || cfg == 8 || cfg == 9) ? 2 : ((cfg == 5 || cfg == 7 || op == 3 || op == 4) ? 1 : 0);
+  return gfpa_cfg_tile(cfg) >= 16 ? 2 : ((gfpa_cfg_tile(cfg) == 8 || op == 3 || op == 4) ? 1 : 0);
 }
 
 // threads per CTA of each class kernel

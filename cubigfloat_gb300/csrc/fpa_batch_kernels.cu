@@ -16,11 +16,11 @@ namespace gfpa {
 
 // One task body per (configuration, operation), out of line so the class kernel is a
 // small dispatcher over separately compiled bodies.
-template <int OP, int G, int K>
+template <int OP, int G, int K, int R>
 __device__ __noinline__ void run_task(const BatchArgs A, uint32_t first, uint32_t count, uint32_t *smem) {
   Grp<G> g;
   constexpr int gpw = 32 / G;
-  constexpr int words = OpWords<OP, G, K>::aligned();
+  constexpr int words = OpWords<OP, G, K, R>::aligned();
   const int warp = (int)(threadIdx.x >> 5), nwarps = (int)(blockDim.x >> 5);
   const int gi = (int)((threadIdx.x & 31u) / G);
   uint32_t *ws = smem + (size_t)warp * A.warp_words + gi * words;
@@ -30,27 +30,32 @@ __device__ __noinline__ void run_task(const BatchArgs A, uint32_t first, uint32_
     const fpa_batch_desc d = A.descs[idx];
     const int n = d.limbs, mode = d.mode;
     if (OP == OP_ADD || OP == OP_SUB)
-      op_addsub<G, K>(g, ws, n, mode, OP == OP_SUB, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx],
+      op_addsub<G, K, R>(g, ws, n, mode, OP == OP_SUB, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx],
                       A.b_limbs + d.b_off, A.r_exps + idx, A.r_limbs + d.r_off);
     else if (OP == OP_MUL)
-      op_mul<G, K>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx], A.b_limbs + d.b_off,
+      op_mul<G, K, R>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx], A.b_limbs + d.b_off,
                    A.r_exps + idx, A.r_limbs + d.r_off);
     else if (OP == OP_DIV)
-      op_div<G, K>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx], A.b_limbs + d.b_off,
+      op_div<G, K, R>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx], A.b_limbs + d.b_off,
                    A.r_exps + idx, A.r_limbs + d.r_off, A.err);
     else
-      op_sqrt<G, K>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.r_exps + idx, A.r_limbs + d.r_off, A.err);
+      op_sqrt<G, K, R>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.r_exps + idx, A.r_limbs + d.r_off, A.err);
     g.sync();
   }
 }
 
-#define GFPA_TASK_OP(CFG, GG, KK, OPV)                                           \
+#define GFPA_TASK_OP(CFG, GG, KK, RR, OPV)                                       \
   case CFG * 5 + OPV:                                                            \
-    if constexpr (gfpa_class_of(CFG, OPV) == CLS) run_task<OPV, GG, KK>(A, t.first, t.count, smem); \
+    if constexpr (gfpa_class_of(CFG, OPV) == CLS) run_task<OPV, GG, KK, RR>(A, t.first, t.count, smem); \
     break;
-#define GFPA_TASK(CFG, GG, KK)                                                   \
-  GFPA_TASK_OP(CFG, GG, KK, OP_ADD) GFPA_TASK_OP(CFG, GG, KK, OP_SUB) GFPA_TASK_OP(CFG, GG, KK, OP_MUL) \
-  GFPA_TASK_OP(CFG, GG, KK, OP_DIV) GFPA_TASK_OP(CFG, GG, KK, OP_SQRT)
+#define GFPA_TASK(CFG, GG, KK, RR)                                               \
+  GFPA_TASK_OP(CFG, GG, KK, RR, OP_ADD) GFPA_TASK_OP(CFG, GG, KK, RR, OP_SUB)    \
+  GFPA_TASK_OP(CFG, GG, KK, RR, OP_MUL) GFPA_TASK_OP(CFG, GG, KK, RR, OP_DIV)    \
+  GFPA_TASK_OP(CFG, GG, KK, RR, OP_SQRT)
+#define GFPA_TASKS_TILE4                                                         \
+  GFPA_TASK(0, 4, 2, 1) GFPA_TASK(1, 8, 2, 1) GFPA_TASK(2, 8, 4, 1) GFPA_TASK(3, 16, 4, 1) \
+  GFPA_TASK(4, 32, 4, 1) GFPA_TASK(10, 8, 4, 2) GFPA_TASK(11, 8, 4, 4) GFPA_TASK(12, 16, 4, 2) \
+  GFPA_TASK(15, 4, 4, 8)
 
 template <int CLS>
 struct ClassShape {
@@ -70,14 +75,14 @@ __global__ void __launch_bounds__(ClassShape<CLS>::threads, ClassShape<CLS>::min
     if (ti >= A.ntasks) break;
     const BatchTask t = A.tasks[ti];
     if constexpr (CLS == 0) {
-      switch (t.key) { GFPA_TASK(0, 4, 2) GFPA_TASK(1, 8, 2) GFPA_TASK(2, 8, 4) GFPA_TASK(3, 16, 4) GFPA_TASK(4, 32, 4) default: break; }
+      switch (t.key) { GFPA_TASKS_TILE4 default: break; }
     } else if constexpr (CLS == 1) {
       switch (t.key) {
-        GFPA_TASK(0, 4, 2) GFPA_TASK(1, 8, 2) GFPA_TASK(2, 8, 4) GFPA_TASK(3, 16, 4) GFPA_TASK(4, 32, 4)
-        GFPA_TASK(5, 32, 8) GFPA_TASK(7, 16, 8) default: break;
+        GFPA_TASKS_TILE4 GFPA_TASK(5, 32, 8, 1) GFPA_TASK(7, 16, 8, 1) GFPA_TASK(13, 8, 8, 4) GFPA_TASK(14, 16, 8, 2)
+        default: break;
       }
     } else {
-      switch (t.key) { GFPA_TASK(6, 32, 16) GFPA_TASK(8, 8, 16) GFPA_TASK(9, 16, 16) default: break; }
+      switch (t.key) { GFPA_TASK(6, 32, 16, 1) GFPA_TASK(8, 8, 16, 1) GFPA_TASK(9, 16, 16, 1) default: break; }
     }
   }
 }

@@ -25,12 +25,12 @@ struct ChainArgs {
   uint32_t *err;
 };
 
-template <int G, int K>
+template <int G, int K, int R>
 struct ChainSpace {
-  static constexpr int N = G * K;
+  static constexpr int N = G * K * R;
   __host__ __device__ static constexpr int cmax(int a, int b) { return a > b ? a : b; }
-  static constexpr int ws_dot = cmax(OpWords<OP_MUL, G, K>::aligned(), OpWords<OP_ADD, G, K>::aligned());
-  static constexpr int ws_newton = cmax(OpWords<OP_DIV, G, K>::aligned(), OpWords<OP_ADD, G, K>::aligned());
+  static constexpr int ws_dot = cmax(OpWords<OP_MUL, G, K, R>::aligned(), OpWords<OP_ADD, G, K, R>::aligned());
+  static constexpr int ws_newton = cmax(OpWords<OP_DIV, G, K, R>::aligned(), OpWords<OP_ADD, G, K, R>::aligned());
   static constexpr int value = N + 8;                   // one number: exponent word + limbs, aligned
   __host__ __device__ static constexpr int dot() { return ws_dot + 2 * value; }
   __host__ __device__ static constexpr int newton() { return ws_newton + 3 * value; }
@@ -45,23 +45,23 @@ __device__ __forceinline__ uint32_t half_of(uint32_t e) {
   return e - 2u;
 }
 
-template <int G, int K>
+template <int G, int K, int R>
 __global__ void __launch_bounds__(128, 4) k_dot(ChainArgs A) {
   extern __shared__ __align__(16) uint32_t smem[];
   Grp<G> g;
-  constexpr int W = ChainSpace<G, K>::dot(), V = ChainSpace<G, K>::value;
+  constexpr int W = ChainSpace<G, K, R>::dot(), V = ChainSpace<G, K, R>::value;
   const uint32_t gpc = blockDim.x / G, gi = threadIdx.x / G;
   uint32_t *ws = smem + gi * W;
-  uint32_t *acc = ws + ChainSpace<G, K>::ws_dot, *tmp = acc + V;   // [0] = exponent, [4..] = limbs
+  uint32_t *acc = ws + ChainSpace<G, K, R>::ws_dot, *tmp = acc + V;   // [0] = exponent, [4..] = limbs
   const int n = (int)A.n;
   for (uint64_t d = (uint64_t)blockIdx.x * gpc + gi; d < A.count; d += (uint64_t)gridDim.x * gpc) {
     if (g.lane == 0) acc[0] = CLS_ZERO;
     g.sync();
     for (uint32_t i = 0; i < A.len; i++) {
       const uint64_t k = d * A.len + i, off = k * (uint64_t)n;
-      op_mul<G, K>(g, ws, n, A.mode, A.x_exps[k], A.x_limbs + off, A.y_exps[k], A.y_limbs + off, tmp, tmp + 4);
+      op_mul<G, K, R>(g, ws, n, A.mode, A.x_exps[k], A.x_limbs + off, A.y_exps[k], A.y_limbs + off, tmp, tmp + 4);
       g.sync();
-      op_addsub<G, K>(g, ws, n, A.mode, 0, acc[0], acc + 4, tmp[0], tmp + 4, acc, acc + 4);
+      op_addsub<G, K, R>(g, ws, n, A.mode, 0, acc[0], acc + 4, tmp[0], tmp + 4, acc, acc + 4);
       g.sync();
     }
     for (int i = g.lane; i < n; i += G) A.r_limbs[d * n + i] = acc[4 + i];
@@ -70,14 +70,14 @@ __global__ void __launch_bounds__(128, 4) k_dot(ChainArgs A) {
   }
 }
 
-template <int G, int K>
+template <int G, int K, int R>
 __global__ void __launch_bounds__(128, 4) k_newton_sqrt(ChainArgs A) {
   extern __shared__ __align__(16) uint32_t smem[];
   Grp<G> g;
-  constexpr int W = ChainSpace<G, K>::newton(), V = ChainSpace<G, K>::value;
+  constexpr int W = ChainSpace<G, K, R>::newton(), V = ChainSpace<G, K, R>::value;
   const uint32_t gpc = blockDim.x / G, gi = threadIdx.x / G;
   uint32_t *ws = smem + gi * W;
-  uint32_t *y = ws + ChainSpace<G, K>::ws_newton, *t = y + V, *s = t + V;
+  uint32_t *y = ws + ChainSpace<G, K, R>::ws_newton, *t = y + V, *s = t + V;
   const int n = (int)A.n;
   for (uint64_t d = (uint64_t)blockIdx.x * gpc + gi; d < A.count; d += (uint64_t)gridDim.x * gpc) {
     const uint64_t off = d * (uint64_t)n;
@@ -86,9 +86,9 @@ __global__ void __launch_bounds__(128, 4) k_newton_sqrt(ChainArgs A) {
     g.sync();
     const uint32_t xe = A.x_exps[d];
     for (uint32_t it = 0; it < A.len; it++) {
-      op_div<G, K>(g, ws, n, A.mode, xe, A.x_limbs + off, y[0], y + 4, t, t + 4, A.err);      // t = x / y
+      op_div<G, K, R>(g, ws, n, A.mode, xe, A.x_limbs + off, y[0], y + 4, t, t + 4, A.err);      // t = x / y
       g.sync();
-      op_addsub<G, K>(g, ws, n, A.mode, 0, y[0], y + 4, t[0], t + 4, s, s + 4);             // s = y + t
+      op_addsub<G, K, R>(g, ws, n, A.mode, 0, y[0], y + 4, t[0], t + 4, s, s + 4);             // s = y + t
       g.sync();
       for (int i = g.lane; i < n; i += G) y[4 + i] = s[4 + i];                              // y = s * 0.5
       if (g.lane == 0) y[0] = half_of(s[0]);
@@ -100,11 +100,11 @@ __global__ void __launch_bounds__(128, 4) k_newton_sqrt(ChainArgs A) {
   }
 }
 
-template <int G, int K>
+template <int G, int K, int R>
 cudaError_t launch_chain(int kind, const ChainArgs &A, cudaStream_t st, int sms) {
   constexpr int gpc = 128 / G;
-  const size_t smem = (size_t)gpc * (kind == 0 ? ChainSpace<G, K>::dot() : ChainSpace<G, K>::newton()) * 4;
-  auto kern = kind == 0 ? k_dot<G, K> : k_newton_sqrt<G, K>;
+  const size_t smem = (size_t)gpc * (kind == 0 ? ChainSpace<G, K, R>::dot() : ChainSpace<G, K, R>::newton()) * 4;
+  auto kern = kind == 0 ? k_dot<G, K, R> : k_newton_sqrt<G, K, R>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per = 0;
@@ -119,13 +119,13 @@ cudaError_t launch_chain(int kind, const ChainArgs &A, cudaStream_t st, int sms)
 
 cudaError_t dispatch_chain(int kind, int cfg, const ChainArgs &A, cudaStream_t st, int sms) {
   switch (cfg) {
-    case 0: return launch_chain<4, 2>(kind, A, st, sms);
-    case 1: return launch_chain<8, 2>(kind, A, st, sms);
-    case 2: return launch_chain<8, 4>(kind, A, st, sms);
-    case 3: return launch_chain<16, 4>(kind, A, st, sms);
-    case 4: return launch_chain<32, 4>(kind, A, st, sms);
-    case 5: return launch_chain<32, 8>(kind, A, st, sms);
-    case 6: return launch_chain<32, 16>(kind, A, st, sms);
+    case 0: return launch_chain<4, 2, 1>(kind, A, st, sms);
+    case 1: return launch_chain<8, 2, 1>(kind, A, st, sms);
+    case 2: return launch_chain<8, 4, 1>(kind, A, st, sms);
+    case 3: return launch_chain<16, 4, 1>(kind, A, st, sms);
+    case 4: return launch_chain<32, 4, 1>(kind, A, st, sms);
+    case 5: return launch_chain<32, 8, 1>(kind, A, st, sms);
+    case 6: return launch_chain<32, 16, 1>(kind, A, st, sms);
   }
   return cudaErrorInvalidValue;
 }

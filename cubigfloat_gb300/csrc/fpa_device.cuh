@@ -8,9 +8,10 @@
 // owns one operation at a time.  Operands are staged in the group's slice of shared
 // memory; big-integer steps (products, adds, compares, rounding) are cooperative over
 // the group, with carries resolved across lanes by ballot-based carry lookahead.
-// Products use product scanning: each lane owns two column blocks of K limbs, paired
-// (t, t+M) so that every lane does the same number of K x K tiles, and accumulates each
-// column in a 96-bit (lo, hi, top) register triple fed by mad.lo.cc / madc.hi.cc.
+// Products use product scanning: the column blocks of K limbs are paired (t, t+M) so that
+// every pair holds the same number of K x K tiles, each lane owns R such pairs (t = lane,
+// lane+G, ...), and each column is accumulated in a 96-bit (lo, hi, top) register triple
+// fed by mad.lo.cc / madc.hi.cc.  A group's capacity is N = G*K*R limbs (G*R <= 32).
 #pragma once
 #include <stdint.h>
 
@@ -216,85 +217,77 @@ __device__ __forceinline__ uint32_t clz32(uint32_t v) { return (uint32_t)__clz((
 
 // ---------------------------------------------------------------------------------------
 // Rounding of a nonnegative integer X[0..xlen) (shared memory) to n limbs.
-// Result limbs: lane owns limbs lane + G*k (k < PER).  Returns false when X == 0.
-// L = bit length of X; ovf = 1 when rounding carried into a new binade.
-template <int G, int PER>
-struct Rounded { uint32_t limb[PER]; int L; int ovf; };
+// grp_round decides the rounding (group-uniform); store_limbs then writes the rounded
+// limbs straight from X, so X must stay unchanged until the store.  Returns false when
+// X == 0.  L = bit length of X; ovf = 1 when rounding carried into a new binade.
+struct Rounded {
+  const uint32_t *X; int xlen;
+  int lo;          // bit index in X of the mantissa's bit 0
+  int L, ovf;
+  int up;          // add one unit in the last place
+  uint32_t f;      // lowest limb that is not all ones (the one the increment stops at)
+};
 
-template <int G, int PER>
+template <int G>
 __device__ bool grp_round(const Grp<G> &g, const uint32_t *X, int xlen, int n, uint32_t sticky_in,
-                          int mode, uint32_t sign, Rounded<G, PER> &out) {
+                          int mode, uint32_t sign, Rounded &out) {
   uint32_t top = 0;
   for (int i = g.lane; i < xlen; i += G) if (X[i]) top = (uint32_t)i + 1u;
   top = g.rmax(top);
   if (top == 0) return false;
-  int h = (int)top - 1;
-  int L = 32 * h + 32 - (int)clz32(X[h]);
-  int lo = L - 32 * n;                              // bit index of the mantissa's bit 0
-  Shifted src{X, xlen, -lo};
-#pragma unroll
-  for (int k = 0; k < PER; k++) {
-    int i = (int)g.lane + G * k;
-    out.limb[k] = (i < n) ? src(i) : 0u;
-  }
-  int rp = lo - 1;                                   // round bit position
+  const int h = (int)top - 1;
+  const int L = 32 * h + 32 - (int)clz32(X[h]);
+  const int lo = L - 32 * n;
+  const Shifted src{X, xlen, -lo};
+  const int rp = lo - 1;                             // round bit position
   uint32_t rbit = 0, st = 0;
   if (rp >= 0) {
     rbit = (X[rp >> 5] >> (rp & 31)) & 1u;
-    int full = rp >> 5;                              // limbs fully below the round limb
+    const int full = rp >> 5;                        // limbs fully below the round limb
     for (int i = g.lane; i < full; i += G) st |= X[i];
     if (g.lane == 0 && (rp & 31)) st |= X[full] & ((1u << (rp & 31)) - 1u);
   }
   st = g.ror(st) | sticky_in;
-  uint32_t lsb = g.bcast(out.limb[0], 0) & 1u;
-  int ovf = 0;
-  if (round_up(mode, sign, lsb, rbit, st != 0)) {
-    uint32_t f = (uint32_t)n;
-#pragma unroll
-    for (int k = 0; k < PER; k++) {
-      int i = (int)g.lane + G * k;
-      if (i < n && out.limb[k] != 0xFFFFFFFFu) f = min(f, (uint32_t)i);
-    }
+  const uint32_t lsb = src(0) & 1u;
+  const int up = round_up(mode, sign, lsb, rbit, st != 0) ? 1 : 0;
+  uint32_t f = (uint32_t)n;
+  if (up) {
+    for (int i = g.lane; i < n; i += G)
+      if (src(i) != 0xFFFFFFFFu) { f = (uint32_t)i; break; }
     f = g.rmin(f);
-#pragma unroll
-    for (int k = 0; k < PER; k++) {
-      int i = (int)g.lane + G * k;
-      if (i < (int)f) out.limb[k] = 0u;
-      else if (i == (int)f) out.limb[k] += 1u;
-    }
-    if (f == (uint32_t)n) {                          // 0.11..1 + ulp = 1.0
-      ovf = 1;
-#pragma unroll
-      for (int k = 0; k < PER; k++) if ((int)g.lane + G * k == n - 1) out.limb[k] = 0x80000000u;
-    }
   }
-  out.L = L; out.ovf = ovf;
+  out.X = X; out.xlen = xlen; out.lo = lo; out.L = L;
+  out.up = up; out.f = f; out.ovf = (up && f == (uint32_t)n) ? 1 : 0;   // 0.11..1 + ulp = 1.0
   return true;
 }
 
-template <int G, int PER>
-__device__ __forceinline__ void store_limbs(const Grp<G> &g, uint32_t *dst, int n, const Rounded<G, PER> &r) {
-#pragma unroll
-  for (int k = 0; k < PER; k++) {
-    int i = (int)g.lane + G * k;
-    if (i < n) dst[i] = r.limb[k];
+template <int G>
+__device__ __forceinline__ void store_limbs(const Grp<G> &g, uint32_t *dst, int n, const Rounded &r) {
+  const Shifted src{r.X, r.xlen, -r.lo};
+  for (int i = g.lane; i < n; i += G) {
+    uint32_t v = src(i);
+    if (r.up) v = (i < (int)r.f) ? 0u : (i == (int)r.f ? v + 1u : v);
+    if (r.ovf && i == n - 1) v = 0x80000000u;
+    dst[i] = v;
   }
 }
 
 // ---------------------------------------------------------------------------------------
-// Square product P[0..2m) = x[0..m) * y[0..m), m <= G*K.
+// Products of up to N = G*K*R limbs per operand.
 //
 // Layout of the per-group product scratch (32-bit words):
-//   sa   : G*K        operand x, zero padded to Mp*K
-//   sb   : G*K + 2K   operand y at offset K, K zero limbs below and above
-//   snap : G*3K       per-lane snapshot of the first block's column sums
-//   part : 2G*(K+2)   per-column-block partial sums (K+2 limbs each)
-template <int G, int K>
+//   sa   : N          operand x, zero padded to Mp*K
+//   sb   : N + 2K     operand y at offset K, K zero limbs below and above
+//   snap : G*3K       per-lane snapshot of the first block's column sums (reused per pair)
+//   part : 2GR*(K+2)  per-column-block partial sums (K+2 limbs each)
+template <int G, int K, int R>
 struct MulScratch {
+  static_assert(G * R <= 32, "the block carry lookahead covers at most 64 column blocks");
+  static constexpr int N = G * K * R;
   uint32_t *sa, *sb, *snap, *part;
-  __host__ __device__ static constexpr int words() { return G * K + (G * K + 2 * K) + G * 3 * K + 2 * G * (K + 2); }
+  __host__ __device__ static constexpr int words() { return N + (N + 2 * K) + G * 3 * K + 2 * G * R * (K + 2); }
   __device__ __forceinline__ void carve(uint32_t *p) {
-    sa = p; sb = sa + G * K; snap = sb + G * K + 2 * K; part = snap + G * 3 * K;
+    sa = p; sb = sa + N; snap = sb + N + 2 * K; part = snap + G * 3 * K;
   }
 };
 
@@ -319,112 +312,114 @@ __device__ __forceinline__ void columns_to_limbs(const uint32_t *lo, const uint3
   }
 }
 
-template <int G, int K>
+template <int G, int K, int R>
 __device__ __forceinline__ void blocks_final_sum_inl(const Grp<G> g, uint32_t *P, int outlen, int Mp,
-                                                     const MulScratch<G, K> s);
+                                                     const MulScratch<G, K, R> s);
 
-// Product P[0..lx+ly) of x (staged in s.sa, Ma = ceil(lx/K) blocks, zero padded) and y
-// (staged in s.sb at offset K, Mb = ceil(ly/K) <= Ma blocks, K zero limbs on each side).
-// Lane t < Ma owns column blocks t and t+Ma.  Block t holds min(t, Mb)+1 tiles and block
-// t+Ma holds max(0, Mb-t), so every lane runs exactly Mb+1 tile steps (for a square, Ma+1).
-// The first block's column sums are snapshotted at the lane's switch step (or after the
-// loop when there is no second block) and the second block is acc - snapshot.
-template <int G, int K>
-__device__ __forceinline__ void grp_mul_staged(const Grp<G> g, uint32_t *P, int lx, int ly, const MulScratch<G, K> s) {
+// Product P[0..lx+ly) of x (staged in s.sa, Mp = ceil(lx/K) blocks, zero padded) and y
+// (staged in s.sb at offset K, Mb = ceil(ly/K) <= Mp blocks, K zero limbs on each side).
+// Pair t < Mp is column blocks t and t+Mp; lane l runs pairs l, l+G, ... in turn.  Block t
+// holds min(t, Mb)+1 tiles and block t+Mp holds max(0, Mb-t), so every pair is exactly
+// Mb+1 tile steps (for a square, Mp+1).  The first block's column sums are snapshotted at
+// the pair's switch step (or after the loop when there is no second block) and the second
+// block is acc - snapshot.
+template <int G, int K, int R>
+__device__ __forceinline__ void grp_mul_staged(const Grp<G> g, uint32_t *P, int lx, int ly, const MulScratch<G, K, R> s) {
   static_assert(K >= 2, "a column block must be at least 2 limbs wide");
   const int Mp = (lx + K - 1) / K, Mb = (ly + K - 1) / K;
-  const int t = (int)g.lane;
-  const bool act = t < Mp;
-  const int n1 = (t < Mb ? t : Mb) + 1;          // tiles of block t
-  const int I0 = t > Mb ? t - Mb : 0;
-  uint32_t lo[K], hi[K], tp[K];
+  uint32_t *sn = s.snap + g.lane * 3 * K;
+#pragma unroll 1
+  for (int pr = 0; pr < R; pr++) {
+    if (pr * G >= Mp) break;                     // uniform over the group
+    const int t = (int)g.lane + pr * G;
+    const bool act = t < Mp;
+    const int n1 = (t < Mb ? t : Mb) + 1;        // tiles of block t
+    const int I0 = t > Mb ? t - Mb : 0;
+    uint32_t lo[K], hi[K], tp[K];
 #pragma unroll
-  for (int c = 0; c < K; c++) { lo[c] = 0; hi[c] = 0; tp[c] = 0; }
-  if (act) {
-    for (int st = 0; st <= Mb; st++) {
-      const bool first = st < n1;
-      const int I = first ? I0 + st : t + Mp - Mb + (st - n1);
-      const int cb = first ? t : t + Mp;
-      if (st == n1) {
-        uint32_t *sn = s.snap + t * 3 * K;
+    for (int c = 0; c < K; c++) { lo[c] = 0; hi[c] = 0; tp[c] = 0; }
+    if (act) {
+      for (int st = 0; st <= Mb; st++) {
+        const bool first = st < n1;
+        const int I = first ? I0 + st : t + Mp - Mb + (st - n1);
+        const int cb = first ? t : t + Mp;
+        if (st == n1) {
+#pragma unroll
+          for (int c = 0; c < K; c++) { sn[c] = lo[c]; sn[K + c] = hi[c]; sn[2 * K + c] = tp[c]; }
+        }
+        uint32_t a[K], w[2 * K];
+        const uint32_t *ap = s.sa + K * I;
+        const uint32_t *wp = s.sb + K * (cb - I);      // w[m] = y[K(cb-I) - K + m]
+        if constexpr (K % 4 == 0) {
+#pragma unroll
+          for (int i = 0; i < K; i += 4) {
+            uint4 v = *reinterpret_cast<const uint4 *>(ap + i);
+            a[i] = v.x; a[i + 1] = v.y; a[i + 2] = v.z; a[i + 3] = v.w;
+          }
+#pragma unroll
+          for (int i = 0; i < 2 * K; i += 4) {
+            uint4 v = *reinterpret_cast<const uint4 *>(wp + i);
+            w[i] = v.x; w[i + 1] = v.y; w[i + 2] = v.z; w[i + 3] = v.w;
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < K; i++) a[i] = ap[i];
+#pragma unroll
+          for (int i = 1; i < 2 * K; i++) w[i] = wp[i];
+        }
+        // column c of this block gets a[i] * y[K(cb-I) + c - i] = a[i] * w[K + c - i]
+#pragma unroll
+        for (int i = 0; i < K; i++)
+#pragma unroll
+          for (int c = 0; c < K; c++) mac3(lo[c], hi[c], tp[c], a[i], w[K + c - i]);
+      }
+      // acc = blocks t + (t+Mp); snapshot = block t.  Emit both as K+2 limbs.
+      if (n1 > Mb) {                             // no second block: snapshot = everything
 #pragma unroll
         for (int c = 0; c < K; c++) { sn[c] = lo[c]; sn[K + c] = hi[c]; sn[2 * K + c] = tp[c]; }
       }
-      uint32_t a[K], w[2 * K];
-      const uint32_t *ap = s.sa + K * I;
-      const uint32_t *wp = s.sb + K * (cb - I);      // w[m] = y[K(cb-I) - K + m]
-      if constexpr (K % 4 == 0) {
+      uint32_t L[K + 2];
+      // second block = acc - snapshot (exact: each column sum < 2^96)
 #pragma unroll
-        for (int i = 0; i < K; i += 4) {
-          uint4 v = *reinterpret_cast<const uint4 *>(ap + i);
-          a[i] = v.x; a[i + 1] = v.y; a[i + 2] = v.z; a[i + 3] = v.w;
-        }
-#pragma unroll
-        for (int i = 0; i < 2 * K; i += 4) {
-          uint4 v = *reinterpret_cast<const uint4 *>(wp + i);
-          w[i] = v.x; w[i + 1] = v.y; w[i + 2] = v.z; w[i + 3] = v.w;
-        }
-      } else {
-#pragma unroll
-        for (int i = 0; i < K; i++) a[i] = ap[i];
-#pragma unroll
-        for (int i = 1; i < 2 * K; i++) w[i] = wp[i];
+      for (int c = 0; c < K; c++) {
+        uint32_t a0 = sn[c], a1 = sn[K + c], a2 = sn[2 * K + c];
+        asm("sub.cc.u32 %0, %0, %3;\n\tsubc.cc.u32 %1, %1, %4;\n\tsubc.u32 %2, %2, %5;"
+            : "+r"(lo[c]), "+r"(hi[c]), "+r"(tp[c]) : "r"(a0), "r"(a1), "r"(a2));
       }
-      // column c of this block gets a[i] * y[K(cb-I) + c - i] = a[i] * w[K + c - i]
+      columns_to_limbs<K>(lo, hi, tp, L);
+      uint32_t *pp = s.part + (t + Mp) * (K + 2);
 #pragma unroll
-      for (int i = 0; i < K; i++)
+      for (int j = 0; j < K + 2; j++) pp[j] = L[j];
 #pragma unroll
-        for (int c = 0; c < K; c++) mac3(lo[c], hi[c], tp[c], a[i], w[K + c - i]);
+      for (int c = 0; c < K; c++) { lo[c] = sn[c]; hi[c] = sn[K + c]; tp[c] = sn[2 * K + c]; }
+      columns_to_limbs<K>(lo, hi, tp, L);
+      pp = s.part + t * (K + 2);
+#pragma unroll
+      for (int j = 0; j < K + 2; j++) pp[j] = L[j];
     }
-  }
-  // lane t: acc = blocks t + (t+Mp); snapshot = block t.  Emit both as K+2 limbs.
-  if (act) {
-    uint32_t *sn = s.snap + t * 3 * K;
-    if (n1 > Mb) {                               // no second block: snapshot = everything
-#pragma unroll
-      for (int c = 0; c < K; c++) { sn[c] = lo[c]; sn[K + c] = hi[c]; sn[2 * K + c] = tp[c]; }
-    }
-    uint32_t L[K + 2];
-    // second block = acc - snapshot (exact: each column sum < 2^96)
-#pragma unroll
-    for (int c = 0; c < K; c++) {
-      uint32_t a0 = sn[c], a1 = sn[K + c], a2 = sn[2 * K + c];
-      asm("sub.cc.u32 %0, %0, %3;\n\tsubc.cc.u32 %1, %1, %4;\n\tsubc.u32 %2, %2, %5;"
-          : "+r"(lo[c]), "+r"(hi[c]), "+r"(tp[c]) : "r"(a0), "r"(a1), "r"(a2));
-    }
-    columns_to_limbs<K>(lo, hi, tp, L);
-    uint32_t *pp = s.part + (t + Mp) * (K + 2);
-#pragma unroll
-    for (int j = 0; j < K + 2; j++) pp[j] = L[j];
-#pragma unroll
-    for (int c = 0; c < K; c++) { lo[c] = sn[c]; hi[c] = sn[K + c]; tp[c] = sn[2 * K + c]; }
-    columns_to_limbs<K>(lo, hi, tp, L);
-    pp = s.part + t * (K + 2);
-#pragma unroll
-    for (int j = 0; j < K + 2; j++) pp[j] = L[j];
   }
   g.sync();
-  blocks_final_sum_inl<G, K>(g, P, lx + ly, Mp, s);
+  blocks_final_sum_inl<G, K, R>(g, P, lx + ly, Mp, s);
 }
 
 // square product of operands staged for m limbs each
-template <int G, int K>
-__device__ __forceinline__ void grp_mulsq_staged(const Grp<G> g, uint32_t *P, int m, const MulScratch<G, K> s) {
-  grp_mul_staged<G, K>(g, P, m, m, s);
+template <int G, int K, int R>
+__device__ __forceinline__ void grp_mulsq_staged(const Grp<G> g, uint32_t *P, int m, const MulScratch<G, K, R> s) {
+  grp_mul_staged<G, K, R>(g, P, m, m, s);
 }
 
 // Out-of-line copy of the product for the operations that call it many times (div, sqrt):
 // one copy of the unrolled tile loop keeps their code inside the instruction cache.
-template <int G, int K>
-__device__ __noinline__ void grp_mul_call(const Grp<G> g, uint32_t *P, int lx, int ly, const MulScratch<G, K> s) {
-  grp_mul_staged<G, K>(g, P, lx, ly, s);
+template <int G, int K, int R>
+__device__ __noinline__ void grp_mul_call(const Grp<G> g, uint32_t *P, int lx, int ly, const MulScratch<G, K, R> s) {
+  grp_mul_staged<G, K, R>(g, P, lx, ly, s);
 }
 
-// P[0..lx+ly) = x[0..lx) * y[0..ly) for functor operands (lx, ly <= G*K, any order): the
+// P[0..lx+ly) = x[0..lx) * y[0..ly) for functor operands (lx, ly <= G*K*R, any order): the
 // longer one is staged as the block operand.
-template <int G, int K, class X, class Y>
+template <int G, int K, int R, class X, class Y>
 __device__ __forceinline__ void grp_mul(const Grp<G> &g, uint32_t *P, X x, int lx, Y y, int ly,
-                                        const MulScratch<G, K> &s) {
+                                        const MulScratch<G, K, R> &s) {
   const bool swap = ly > lx;
   const int la = swap ? ly : lx, lb = swap ? lx : ly;
   const int Ma = (la + K - 1) / K, Mb = (lb + K - 1) / K;
@@ -434,67 +429,75 @@ __device__ __forceinline__ void grp_mul(const Grp<G> &g, uint32_t *P, X x, int l
     s.sb[i] = (j >= 0 && j < lb) ? (swap ? x(j) : y(j)) : 0u;
   }
   g.sync();
-  grp_mul_call<G, K>(g, P, la, lb, s);
+  grp_mul_call<G, K, R>(g, P, la, lb, s);
 }
 
 // Sum of the per-block partials (K+2 limbs at block offsets K*cb) into P[0..outlen).
-// Lane t < Mp owns blocks t and t+Mp; carries between blocks by ballot lookahead.
-template <int G, int K>
+// Each block cb = part[cb][0..K) + part[cb-1][K..K+2) is written without its carry in;
+// the carries between the 2*Mp <= 64 blocks come from one 64-bit lookahead over the
+// generate / propagate ballots, and the (rare) blocks that receive one are incremented.
+template <int G, int K, int R>
 __device__ __forceinline__ void blocks_final_sum_inl(const Grp<G> g, uint32_t *P, int outlen, int Mp,
-                                                     const MulScratch<G, K> s) {
-  const int t = (int)g.lane;
-  const bool act = t < Mp;
-  // block cb = part[cb][0..K) + part[cb-1][K..K+2)
-  uint32_t V0[K], V1[K];
-  uint32_t g0 = 0, g1 = 0, p0 = 0, p1 = 0;
-  if (act) {
+                                                     const MulScratch<G, K, R> s) {
+  uint64_t Gm = 0, Pm = 0;
+#pragma unroll
+  for (int pr = 0; pr < R; pr++) {
+    if (pr * G >= Mp) break;                     // uniform over the group
+    const int t = (int)g.lane + pr * G;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
       const int cb = t + half * Mp;
-      const uint32_t *pc = s.part + cb * (K + 2);
-      uint32_t c0 = 0, c1 = 0;
-      if (cb > 0) { c0 = s.part[(cb - 1) * (K + 2) + K]; c1 = s.part[(cb - 1) * (K + 2) + K + 1]; }
-      uint64_t carry = 0;
-      uint32_t all1 = 1u;
-      uint32_t *V = half ? V1 : V0;
+      uint32_t gen = 0, prop = 0;
+      if (t < Mp) {
+        const uint32_t *pc = s.part + cb * (K + 2);
+        uint32_t c0 = 0, c1 = 0;
+        if (cb > 0) { c0 = s.part[(cb - 1) * (K + 2) + K]; c1 = s.part[(cb - 1) * (K + 2) + K + 1]; }
+        uint64_t carry = 0;
+        uint32_t all1 = 1u;
 #pragma unroll
-      for (int j = 0; j < K; j++) {
-        uint64_t sum = (uint64_t)pc[j] + carry + (j == 0 ? c0 : 0u) + (j == 1 ? c1 : 0u);
-        V[j] = (uint32_t)sum; carry = sum >> 32;
-        all1 &= (V[j] == 0xFFFFFFFFu);
+        for (int j = 0; j < K; j++) {
+          const uint64_t sum = (uint64_t)pc[j] + carry + (j == 0 ? c0 : 0u) + (j == 1 ? c1 : 0u);
+          const uint32_t v = (uint32_t)sum;
+          carry = sum >> 32;
+          all1 &= (v == 0xFFFFFFFFu);
+          const int idx = K * cb + j;
+          if (idx < outlen) P[idx] = v;
+        }
+        gen = (uint32_t)(carry != 0);
+        prop = all1 && carry == 0;
       }
-      if (half) { g1 = (uint32_t)(carry != 0); p1 = all1 && carry == 0; }
-      else { g0 = (uint32_t)(carry != 0); p0 = all1 && carry == 0; }
+      const uint32_t bg = g.ballot(gen), bp = g.ballot(prop);
+      const int sh = pr * G + half * Mp;         // bit of lane l = block l + sh
+      if (sh < 64) { Gm |= (uint64_t)bg << sh; Pm |= (uint64_t)bp << sh; }
     }
   }
-  uint32_t bg0 = g.ballot(g0), bg1 = g.ballot(g1), bp0 = g.ballot(p0), bp1 = g.ballot(p1);
-  const uint64_t lowm = (Mp >= 64) ? ~0ull : ((1ull << Mp) - 1ull);
-  uint64_t Gm = ((uint64_t)bg0 & lowm) | ((uint64_t)bg1 << Mp);
-  uint64_t Pm = ((uint64_t)bp0 & lowm) | ((uint64_t)bp1 << Mp);
-  uint64_t A = Gm | Pm, B = Gm;
-  uint64_t cv = (A + B) ^ A ^ B;
-  if (act) {
+  const uint64_t A = Gm | Pm, B = Gm;
+  const uint64_t cv = (A + B) ^ A ^ B;           // bit cb = carry into block cb
+#pragma unroll
+  for (int pr = 0; pr < R; pr++) {
+    if (pr * G >= Mp) break;
+    const int t = (int)g.lane + pr * G;
 #pragma unroll
     for (int half = 0; half < 2; half++) {
       const int cb = t + half * Mp;
-      uint32_t *V = half ? V1 : V0;
-      uint32_t cin = (uint32_t)(cv >> cb) & 1u;
-#pragma unroll
-      for (int j = 0; j < K; j++) {
-        uint32_t v = V[j] + cin;
-        cin = cin && (v == 0u);
-        const int idx = K * cb + j;
-        if (idx < outlen) P[idx] = v;
+      if (t < Mp && ((cv >> cb) & 1u)) {
+        for (int j = 0; j < K; j++) {
+          const int idx = K * cb + j;
+          if (idx >= outlen) break;
+          const uint32_t v = P[idx] + 1u;
+          P[idx] = v;
+          if (v) break;
+        }
       }
     }
   }
   g.sync();
 }
 
-// P[0..2m) = x[0..m) * y[0..m) with x, y functors (any storage); m <= G*K
-template <int G, int K, class X, class Y>
-__device__ __forceinline__ void grp_mulsq(const Grp<G> &g, uint32_t *P, X x, Y y, int m, const MulScratch<G, K> &s) {
-  grp_mul<G, K>(g, P, x, m, y, m, s);
+// P[0..2m) = x[0..m) * y[0..m) with x, y functors (any storage); m <= G*K*R
+template <int G, int K, int R, class X, class Y>
+__device__ __forceinline__ void grp_mulsq(const Grp<G> &g, uint32_t *P, X x, Y y, int m, const MulScratch<G, K, R> &s) {
+  grp_mul<G, K, R>(g, P, x, m, y, m, s);
 }
 
 }  // namespace gfpa

@@ -1,8 +1,8 @@
 // fpa_kernels.cu -- elementwise fpa kernels for one lane-group configuration.
 //
-// This file is compiled once per configuration (GFPA_CFG selects G lanes per operation
-// and K limbs per product tile, capacity N = G*K limbs) so the configurations build in
-// parallel.  Each object exports gfpa_launch_cfg<i>() used by the host dispatcher.
+// This file is compiled once per configuration (GFPA_CFG selects G lanes per operation,
+// K limbs per product tile and R column-block pairs per lane, capacity N = G*K*R limbs)
+// so the configurations build in parallel.  Each object exports gfpa_launch_cfg<i>() used by the host dispatcher.
 #include <cuda_runtime.h>
 #include "fpa_ops.cuh"
 #include "fpa_launch.h"
@@ -14,33 +14,67 @@
 #if GFPA_CFG == 0
 #define CFG_G 4
 #define CFG_K 2
+#define CFG_R 1
 #elif GFPA_CFG == 1
 #define CFG_G 8
 #define CFG_K 2
+#define CFG_R 1
 #elif GFPA_CFG == 2
 #define CFG_G 8
 #define CFG_K 4
+#define CFG_R 1
 #elif GFPA_CFG == 3
 #define CFG_G 16
 #define CFG_K 4
+#define CFG_R 1
 #elif GFPA_CFG == 4
 #define CFG_G 32
 #define CFG_K 4
+#define CFG_R 1
 #elif GFPA_CFG == 5
 #define CFG_G 32
 #define CFG_K 8
+#define CFG_R 1
 #elif GFPA_CFG == 6
 #define CFG_G 32
 #define CFG_K 16
+#define CFG_R 1
 #elif GFPA_CFG == 7
 #define CFG_G 16
 #define CFG_K 8
+#define CFG_R 1
 #elif GFPA_CFG == 8
 #define CFG_G 8
 #define CFG_K 16
+#define CFG_R 1
 #elif GFPA_CFG == 9
 #define CFG_G 16
 #define CFG_K 16
+#define CFG_R 1
+#elif GFPA_CFG == 10
+#define CFG_G 8
+#define CFG_K 4
+#define CFG_R 2
+#elif GFPA_CFG == 11
+#define CFG_G 8
+#define CFG_K 4
+#define CFG_R 4
+#elif GFPA_CFG == 12
+#define CFG_G 16
+#define CFG_K 4
+#define CFG_R 2
+#elif GFPA_CFG == 13
+#define CFG_G 8
+#define CFG_K 8
+#define CFG_R 4
+#elif GFPA_CFG == 14
+#define CFG_G 16
+#define CFG_K 8
+#define CFG_R 2
+#elif GFPA_CFG == 15
+#define CFG_G 4
+#define CFG_K 4
+#define CFG_R 8
 #else
 #error "unknown GFPA_CFG"
 #endif
@@ -51,8 +85,8 @@
 
 namespace gfpa {
 
-template <int OP, int G, int K>
-using Words = OpWords<OP, G, K>;
+template <int OP, int G, int K, int R>
+using Words = OpWords<OP, G, K, R>;
 
 // Register budgets (blocks of 128 threads per SM): 64 registers per thread for add/sub/mul
 // with tiles up to 4 limbs, 128 for 8-limb tiles and for div/sqrt (whose Newton loops keep
@@ -66,40 +100,46 @@ struct MinBlocks {
                            : ((OP == OP_DIV || OP == OP_SQRT) ? (K >= 8 ? 4 : GFPA_NEWTON_MINBLOCKS) : (K >= 8 ? 4 : 8));
 };
 
-template <int OP, int G, int K>
+template <int OP, int G, int K, int R>
 __global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(ElementwiseArgs args) {
   extern __shared__ __align__(16) uint32_t smem[];
   Grp<G> g;
   const uint32_t gpc = blockDim.x / G, gi = threadIdx.x / G;
-  uint32_t *ws = smem + gi * Words<OP, G, K>::aligned();
+  uint32_t *ws = smem + gi * Words<OP, G, K, R>::aligned();
   const int n = (int)args.n;
   for (uint64_t i = (uint64_t)blockIdx.x * gpc + gi; i < args.count; i += (uint64_t)gridDim.x * gpc) {
     const uint64_t off = i * (uint64_t)n;
     const uint32_t a_exp = args.a_exps[i];
     const uint32_t b_exp = (OP == OP_SQRT) ? 0u : args.b_exps[i];
     if (OP == OP_ADD || OP == OP_SUB)
-      op_addsub<G, K>(g, ws, n, args.mode, OP == OP_SUB, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
+      op_addsub<G, K, R>(g, ws, n, args.mode, OP == OP_SUB, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
                       args.r_exps + i, args.r_limbs + off);
     else if (OP == OP_MUL)
-      op_mul<G, K>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
+      op_mul<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
                    args.r_exps + i, args.r_limbs + off);
     else if (OP == OP_DIV)
-      op_div<G, K>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
+      op_div<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
                    args.r_exps + i, args.r_limbs + off, args.err);
     else
-      op_sqrt<G, K>(g, ws, n, args.mode, a_exp, args.a_limbs + off, args.r_exps + i, args.r_limbs + off, args.err);
+      op_sqrt<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, args.r_exps + i, args.r_limbs + off, args.err);
     g.sync();   // the group's shared slice is reused by its next instance
   }
 }
 
 template <int OP>
 static cudaError_t launch_op(const ElementwiseArgs &args, cudaStream_t stream, int sms) {
-  constexpr int G = CFG_G, K = CFG_K;
-  constexpr int threads = 128;
+  constexpr int G = CFG_G, K = CFG_K, R = CFG_R;
+  // four warps per CTA, fewer when one warp's groups need more than a quarter of the
+  // 227 KB a CTA may use
+  constexpr size_t warp_bytes = (size_t)(32 / G) * Words<OP, G, K, R>::aligned() * sizeof(uint32_t);
+  constexpr size_t cta_max = 227 * 1024;
+  if constexpr (warp_bytes > cta_max) return cudaErrorInvalidConfiguration;
+  constexpr int warps = warp_bytes * 4 <= cta_max ? 4 : (warp_bytes * 2 <= cta_max ? 2 : 1);
+  constexpr int threads = 32 * warps;
   constexpr int gpc = threads / G;
-  const size_t smem = (size_t)gpc * Words<OP, G, K>::aligned() * sizeof(uint32_t);
+  const size_t smem = (size_t)warps * warp_bytes;
   static int configured = 0, per_sm = 1;
-  auto kern = k_elementwise<OP, G, K>;
+  auto kern = k_elementwise<OP, G, K, R>;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -17,15 +17,18 @@ struct ElementwiseArgs {
   uint32_t *err;
 };
 
-#define GFPA_NUM_CFGS 10
+#define GFPA_NUM_CFGS 16
 #define GFPA_NUM_DEFAULT_CFGS 7
 #define GFPA_MAX_LIMBS 512
 
-// Lane-group configurations (G lanes x K limbs per tile, capacity G*K limbs).  0..6 are
-// the defaults in increasing capacity; 7..9 use fewer lanes with wider tiles so that two
-// or four operations share a warp, which the autotuner can choose (for div/sqrt).
-static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16};
-static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16};
+// Lane-group configurations (G lanes x K limbs per tile x R block pairs per lane, capacity
+// G*K*R limbs).  0..6 are the defaults in increasing capacity; 7..15 put two to eight
+// operations in one warp (fewer lanes per operation, wider tiles or several block pairs
+// per lane), which the autotuner can choose (mostly for div/sqrt).
+static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4};
+static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4};
+static const int gfpa_cfg_R[GFPA_NUM_CFGS] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 2, 4, 2, 8};
+static inline int gfpa_cfg_capacity(int c) { return gfpa_cfg_G[c] * gfpa_cfg_K[c] * gfpa_cfg_R[c]; }
 
 extern "C" {
 cudaError_t gfpa_launch_cfg0(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
@@ -38,12 +41,18 @@ cudaError_t gfpa_launch_cfg6(int op, const ElementwiseArgs *args, cudaStream_t s
 cudaError_t gfpa_launch_cfg7(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 cudaError_t gfpa_launch_cfg8(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 cudaError_t gfpa_launch_cfg9(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg10(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg11(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg12(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg13(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg14(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg15(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 }
 
 // smallest default configuration whose capacity holds n limbs
 static inline int gfpa_default_cfg(uint32_t n) {
   for (int c = 0; c < GFPA_NUM_DEFAULT_CFGS; c++)
-    if ((uint32_t)(gfpa_cfg_G[c] * gfpa_cfg_K[c]) >= n) return c;
+    if ((uint32_t)gfpa_cfg_capacity(c) >= n) return c;
   return -1;
 }
 
@@ -59,6 +68,12 @@ static inline cudaError_t gfpa_launch(int cfg, int op, const ElementwiseArgs *ar
     case 7: return gfpa_launch_cfg7(op, args, stream, sms);
     case 8: return gfpa_launch_cfg8(op, args, stream, sms);
     case 9: return gfpa_launch_cfg9(op, args, stream, sms);
+    case 10: return gfpa_launch_cfg10(op, args, stream, sms);
+    case 11: return gfpa_launch_cfg11(op, args, stream, sms);
+    case 12: return gfpa_launch_cfg12(op, args, stream, sms);
+    case 13: return gfpa_launch_cfg13(op, args, stream, sms);
+    case 14: return gfpa_launch_cfg14(op, args, stream, sms);
+    case 15: return gfpa_launch_cfg15(op, args, stream, sms);
   }
   return cudaErrorInvalidValue;
 }

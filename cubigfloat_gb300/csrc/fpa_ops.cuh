@@ -10,10 +10,10 @@
 
 namespace gfpa {
 
-// Workspace words per group, beyond MulScratch.  N = G*K is the group's limb capacity.
-template <int G, int K>
+// Workspace words per group, beyond MulScratch.  N = G*K*R is the group's limb capacity.
+template <int G, int K, int R>
 struct OpSpace {
-  static constexpr int N = G * K;
+  static constexpr int N = G * K * R;
   __host__ __device__ static constexpr int addsub() { return 3 * N + 8; }
   __host__ __device__ static constexpr int mul() { return 2 * N + 4; }
   __host__ __device__ static constexpr int div() { return 2 * N + (N + 4) * 2 + (2 * N + 8) * 2 + (N + 8) * 3; }
@@ -23,25 +23,25 @@ struct OpSpace {
     int m = a > b ? a : b; m = m > c ? m : c; m = m > d ? m : d;
     return m;
   }
-  __host__ __device__ static constexpr int words() { return MulScratch<G, K>::words() + max_all(); }
+  __host__ __device__ static constexpr int words() { return MulScratch<G, K, R>::words() + max_all(); }
 };
 
 // Shared-memory words one group needs for operation OP (16-byte aligned slice size).
-template <int OP, int G, int K>
+template <int OP, int G, int K, int R>
 struct OpWords {
   __host__ __device__ static constexpr int v() {
-    return (OP == OP_ADD || OP == OP_SUB) ? OpSpace<G, K>::addsub()
-           : MulScratch<G, K>::words() + (OP == OP_MUL ? OpSpace<G, K>::mul()
-                                          : OP == OP_DIV ? OpSpace<G, K>::div() : OpSpace<G, K>::sqrt());
+    return (OP == OP_ADD || OP == OP_SUB) ? OpSpace<G, K, R>::addsub()
+           : MulScratch<G, K, R>::words() + (OP == OP_MUL ? OpSpace<G, K, R>::mul()
+                                          : OP == OP_DIV ? OpSpace<G, K, R>::div() : OpSpace<G, K, R>::sqrt());
   }
   __host__ __device__ static constexpr int aligned() { return (v() + 3) & ~3; }
 };
 
 // Rounded mantissa + exponent for one instance, written by the group.
-template <int G, int PER>
+template <int G>
 __device__ __forceinline__ void write_value(const Grp<G> &g, uint32_t *r_exp, uint32_t *r, int n,
-                                            const Rounded<G, PER> &res, uint32_t exp_word) {
-  store_limbs<G, PER>(g, r, n, res);
+                                            const Rounded &res, uint32_t exp_word) {
+  store_limbs<G>(g, r, n, res);
   if (g.lane == 0) *r_exp = exp_word;
 }
 
@@ -71,11 +71,11 @@ __device__ __forceinline__ uint32_t exp_word(long long e, uint32_t sign) {
 // (X, X+1) (d > 64 implies at most one bit of cancellation, so 63 guard bits remain).
 // Range: effective add -> +-INF when BIAS+e > 0x7FFFFFFF (:118-119); effective
 // subtraction -> +-TINY when BIAS+e < 5 (:226-227, :272-273).
-template <int G, int K>
+template <int G, int K, int R>
 __device__ void op_addsub(const Grp<G> &g, uint32_t *ws, int n, int mode, int is_sub,
                           uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
                           uint32_t *r_exp, uint32_t *r) {
-  constexpr int N = G * K;
+  constexpr int N = G * K * R;
   const uint32_t act = c_action[is_sub][classify(a_exp) * 9 + classify(b_exp)];
   if (act == ACT_COPY_A) { copy_value<G>(g, r_exp, r, n, a_exp, a); return; }
   if (act == ACT_COPY_B) { copy_value<G>(g, r_exp, r, n, b_exp, b); return; }
@@ -112,37 +112,37 @@ __device__ void op_addsub(const Grp<G> &g, uint32_t *ws, int n, int mode, int is
   Shifted bigs{big, n, 64}, smls{sml, n, 64 - d};
   if (eff_sub) grp_sub<G>(g, X, bigs, smls, xl, lost);
   else grp_add<G>(g, X, bigs, smls, xl, 0u);
-  Rounded<G, K + 1> res;
-  if (!grp_round<G, K + 1>(g, X, xl, n, lost, mode, sign, res)) { write_class<G>(g, r_exp, CLS_ZERO); return; }
+  Rounded res;
+  if (!grp_round<G>(g, X, xl, n, lost, mode, sign, res)) { write_class<G>(g, r_exp, CLS_ZERO); return; }
   const long long e = ebig - 32LL * n - 64 + res.L + res.ovf;
   if (!eff_sub && (long long)BIAS + e > 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
   if (eff_sub && (long long)BIAS + e < 5) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
-  write_value<G, K + 1>(g, r_exp, r, n, res, exp_word(e, sign));
+  write_value<G>(g, r_exp, r, n, res, exp_word(e, sign));
 }
 
 // ---------------------------------------------------------------------------------------
 // mul.  Reference: fpa_warp_mul.h:41-139.  Exact 2n-limb product, one rounding.
 // Range (:124-128): TINY when BIAS+e < 5, INF when BIAS+e > 0x7FFFFFFF.
-template <int G, int K>
+template <int G, int K, int R>
 __device__ void op_mul(const Grp<G> &g, uint32_t *ws, int n, int mode,
                        uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
                        uint32_t *r_exp, uint32_t *r) {
   const uint32_t act = c_action[2][classify(a_exp) * 9 + classify(b_exp)];
   if (act != ACT_MUL) { write_class<G>(g, r_exp, act); return; }
-  MulScratch<G, K> s; s.carve(ws);
-  uint32_t *P = ws + MulScratch<G, K>::words();
+  MulScratch<G, K, R> s; s.carve(ws);
+  uint32_t *P = ws + MulScratch<G, K, R>::words();
   const int Mp = (n + K - 1) / K, NK = Mp * K;
   for (int i = g.lane; i < NK; i += G) s.sa[i] = (i < n) ? a[i] : 0u;
   for (int i = g.lane; i < NK + 2 * K; i += G) { int j = i - K; s.sb[i] = (j >= 0 && j < n) ? b[j] : 0u; }
   g.sync();
-  grp_mulsq_staged<G, K>(g, P, n, s);
+  grp_mulsq_staged<G, K, R>(g, P, n, s);
   const uint32_t sign = (a_exp ^ b_exp) & 1u;
-  Rounded<G, K> res;
-  grp_round<G, K>(g, P, 2 * n, n, 0u, mode, sign, res);
+  Rounded res;
+  grp_round<G>(g, P, 2 * n, n, 0u, mode, sign, res);
   const long long e = (long long)(a_exp >> 1) + (long long)(b_exp >> 1) - 2LL * BIAS - 64LL * n + res.L + res.ovf;
   if ((long long)BIAS + e < 5) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
   if ((long long)BIAS + e > 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
-  write_value<G, K>(g, r_exp, r, n, res, exp_word(e, sign));
+  write_value<G>(g, r_exp, r, n, res, exp_word(e, sign));
 }
 
 // ---------------------------------------------------------------------------------------
@@ -200,18 +200,18 @@ struct ResidualMag {
 //   3. X = 2Q + [2R >= B], sticky = R != 0 (2R == B is impossible for a quotient of two
 //      precision-p numbers), rounded once.
 // Range (:189-193): TINY when BIAS+e < 10, INF when BIAS+e >= 0x7FFFFFFF.
-template <int G, int K>
+template <int G, int K, int R>
 __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
                        uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
                        uint32_t *r_exp, uint32_t *r, uint32_t *err) {
-  constexpr int N = G * K;
+  constexpr int N = G * K * R;
   const uint32_t act = c_action[3][classify(a_exp) * 9 + classify(b_exp)];
   if (act != ACT_DIV) { write_class<G>(g, r_exp, act); return; }
-  MulScratch<G, K> s; s.carve(ws);
-  uint32_t *sA = ws + MulScratch<G, K>::words(), *sB = sA + N;
+  MulScratch<G, K, R> s; s.carve(ws);
+  uint32_t *sA = ws + MulScratch<G, K, R>::words(), *sB = sA + N;
   uint32_t *Y = sB + N, *Y2 = Y + (N + 4);
   uint32_t *T = Y2 + (N + 4), *P2 = T + (2 * N + 8);
-  uint32_t *Q = P2 + (2 * N + 8), *R = Q + (N + 8), *X = R + (N + 8);
+  uint32_t *Q = P2 + (2 * N + 8), *Rm = Q + (N + 8), *X = Rm + (N + 8);
   for (int i = g.lane; i < n; i += G) { sA[i] = a[i]; sB[i] = b[i]; }
   if (g.lane == 0) {
     uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)b[n - 1];   // level 1: floor((2^64-1)/B_top)
@@ -224,11 +224,11 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
     const int k = lv[li - 1], kp = lv[li];
     const uint32_t *Bk = sB + (n - kp);
     // T = B_k' * Y_k   (k' x (k+1) limbs)
-    grp_mul<G, K>(g, T, Ptr{Bk, kp}, kp, Ptr{Y, k + 1}, k + 1, s);
+    grp_mul<G, K, R>(g, T, Ptr{Bk, kp}, kp, Ptr{Y, k + 1}, k + 1, s);
     // M = (Y_k * (|E| >> 32(k-1))) >> 32(k+1)
     const int L = k + kp, lt = kp - k + 3;
     const uint32_t neg = T[L] != 0u;
-    grp_mul<G, K>(g, P2, Ptr{Y, k + 1}, k + 1, ResidualMag{T, k - 1, L, lt, neg}, lt, s);
+    grp_mul<G, K, R>(g, P2, Ptr{Y, k + 1}, k + 1, ResidualMag{T, k - 1, L, lt, neg}, lt, s);
     // Y_k' = Y_k * 2^(32(k'-k)) +- M   (E <= 0 means Y_k was too large)
     Shifted ysh{Y, k + 1, 32 * (kp - k)};
     Ptr M{P2 + (k + 1), lt};
@@ -238,43 +238,43 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   }
   // Q = floor(A * Y / 2^(32n)),  n+1 limbs;  Y = ytop*2^(32n) + Ylow
   const uint32_t ytop = Y[n];
-  grp_mulsq<G, K>(g, T, Ptr{sA, n}, Ptr{Y, n}, n, s);
+  grp_mulsq<G, K, R>(g, T, Ptr{sA, n}, Ptr{Y, n}, n, s);
   if (g.lane == 0) { T[2 * n] = 0; T[2 * n + 1] = 0; }
   g.sync();
   grp_add<G>(g, T + n, Ptr{T + n, n + 2}, SmallMul{sA, n, ytop}, n + 2, 0u);
   grp_copy<G>(g, Q, Ptr{T + n, n + 2}, n + 1);
-  // R = (A * 2^(32n) - Q * B) mod 2^(32(n+2))
+  // Rm = (A * 2^(32n) - Q * B) mod 2^(32(n+2))
   const uint32_t qtop = Q[n];
-  grp_mulsq<G, K>(g, P2, Ptr{Q, n}, Ptr{sB, n}, n, s);
+  grp_mulsq<G, K, R>(g, P2, Ptr{Q, n}, Ptr{sB, n}, n, s);
   if (g.lane == 0) { P2[2 * n] = 0; P2[2 * n + 1] = 0; P2[2 * n + 2] = 0; }
   g.sync();
   grp_add<G>(g, P2 + n, Ptr{P2 + n, n + 3}, SmallMul{sB, n, qtop}, n + 3, 0u);
-  grp_sub<G>(g, R, Shifted{sA, n, 32 * n}, Ptr{P2, 2 * n + 3}, n + 2, 0u);
-  // exact correction: 0 <= R < B
+  grp_sub<G>(g, Rm, Shifted{sA, n, 32 * n}, Ptr{P2, 2 * n + 3}, n + 2, 0u);
+  // exact correction: 0 <= Rm < B
   int guard = 0;
-  while ((R[n + 1] >> 31) != 0 && guard < 64) {
+  while ((Rm[n + 1] >> 31) != 0 && guard < 64) {
     grp_sub<G>(g, Q, Ptr{Q, n + 1}, Zero{}, n + 1, 1u);
-    grp_add<G>(g, R, Ptr{R, n + 2}, Ptr{sB, n}, n + 2, 0u);
+    grp_add<G>(g, Rm, Ptr{Rm, n + 2}, Ptr{sB, n}, n + 2, 0u);
     guard++;
   }
-  while (grp_cmp<G>(g, Ptr{R, n + 2}, Ptr{sB, n}, n + 2) >= 0 && guard < 64) {
+  while (grp_cmp<G>(g, Ptr{Rm, n + 2}, Ptr{sB, n}, n + 2) >= 0 && guard < 64) {
     grp_add<G>(g, Q, Ptr{Q, n + 1}, Zero{}, n + 1, 1u);
-    grp_sub<G>(g, R, Ptr{R, n + 2}, Ptr{sB, n}, n + 2, 0u);
+    grp_sub<G>(g, Rm, Ptr{Rm, n + 2}, Ptr{sB, n}, n + 2, 0u);
     guard++;
   }
   if (guard >= 64 && g.lane == 0) atomicOr(err, 1u);
-  const int c2 = grp_cmp<G>(g, ShlBits{R, n + 2, 1}, Ptr{sB, n}, n + 2);
+  const int c2 = grp_cmp<G>(g, ShlBits{Rm, n + 2, 1}, Ptr{sB, n}, n + 2);
   const uint32_t rb = c2 >= 0 ? 1u : 0u;
-  const uint32_t sticky = (!grp_is_zero<G>(g, Ptr{R, n + 2}, n + 2) && c2 != 0) ? 1u : 0u;
+  const uint32_t sticky = (!grp_is_zero<G>(g, Ptr{Rm, n + 2}, n + 2) && c2 != 0) ? 1u : 0u;
   // X = 2Q + rb  (n+2 limbs)
   grp_add<G>(g, X, ShlBits{Q, n + 1, 1}, Zero{}, n + 2, rb);
   const uint32_t sign = (a_exp ^ b_exp) & 1u;
-  Rounded<G, K + 1> res;
-  grp_round<G, K + 1>(g, X, n + 2, n, sticky, mode, sign, res);
+  Rounded res;
+  grp_round<G>(g, X, n + 2, n, sticky, mode, sign, res);
   const long long e = (long long)(a_exp >> 1) - (long long)(b_exp >> 1) - 32LL * n - 1 + res.L + res.ovf;
   if ((long long)BIAS + e < 10) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
   if ((long long)BIAS + e >= 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
-  write_value<G, K + 1>(g, r_exp, r, n, res, exp_word(e, sign));
+  write_value<G>(g, r_exp, r, n, res, exp_word(e, sign));
 }
 
 // integer square root of a 64-bit value (bitwise, exact)
@@ -297,18 +297,18 @@ __device__ __forceinline__ uint64_t isqrt64(uint64_t x) {
 //   2. S = floor(A * Z / 2^(32n [+1])), one exact correction with R = A_ext - S^2 until
 //      0 <= R <= 2S.
 //   3. X = 2S + [R > S], sticky = R != 0, rounded once (positive).
-template <int G, int K>
+template <int G, int K, int R>
 __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
                         uint32_t a_exp, const uint32_t *a, uint32_t *r_exp, uint32_t *r, uint32_t *err) {
-  constexpr int N = G * K;
+  constexpr int N = G * K * R;
   const uint32_t act = c_sqrt_action[classify(a_exp)];
   if (act != ACT_SQRT) { write_class<G>(g, r_exp, act); return; }
-  MulScratch<G, K> s; s.carve(ws);
-  uint32_t *sA = ws + MulScratch<G, K>::words();
+  MulScratch<G, K, R> s; s.carve(ws);
+  uint32_t *sA = ws + MulScratch<G, K, R>::words();
   uint32_t *X2 = sA + N;                       // A_ext, 2n limbs
   uint32_t *Z = X2 + (2 * N + 4), *Z2 = Z + (N + 4);
   uint32_t *W = Z2 + (N + 4), *V1 = W + (2 * N + 8), *V2 = V1 + (2 * N + 8), *P = V2 + (2 * N + 8);
-  uint32_t *E = P + (2 * N + 8), *S = E + (2 * N + 8), *R = S + (N + 8);
+  uint32_t *E = P + (2 * N + 8), *S = E + (2 * N + 8), *Rm = S + (N + 8);
   const long long e = (long long)(a_exp >> 1) - BIAS;
   const int odd = (int)(e & 1);
   const long long h = (e + odd) / 2;           // exact: e + odd is even
@@ -327,18 +327,18 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   for (int li = 1; li < nl; li++) {
     const int k = lv[li - 1], kp = lv[li];
     // W = Z_k^2  (Z_k has k+1 limbs)
-    grp_mulsq<G, K>(g, W, Ptr{Z, k + 1}, Ptr{Z, k + 1}, k + 1, s);
+    grp_mulsq<G, K, R>(g, W, Ptr{Z, k + 1}, Ptr{Z, k + 1}, k + 1, s);
     // V = X_k' * W = X*W[0..k') + (X*W[k'..2k+2)) << k'   (the second factor is short)
     const uint32_t *Xk = X2 + (2 * n - kp);
     const int ls = 2 * k + 2 - kp;
-    grp_mulsq<G, K>(g, V1, Ptr{Xk, kp}, Ptr{W, kp}, kp, s);
-    grp_mul<G, K>(g, V2, Ptr{Xk, kp}, kp, Ptr{W + kp, ls}, ls, s);
+    grp_mulsq<G, K, R>(g, V1, Ptr{Xk, kp}, Ptr{W, kp}, kp, s);
+    grp_mul<G, K, R>(g, V2, Ptr{Xk, kp}, kp, Ptr{W + kp, ls}, ls, s);
     const int L = kp + 2 * k, lenV = L + 1;
     grp_add<G>(g, V1, Ptr{V1, 2 * kp}, Shifted{V2, kp + ls, 32 * kp}, lenV, 0u);
     // M = (Z_k * (|E| >> 32(2k-1))) >> (32(k+1) + 1),  E = 2^(32L) - V
     const int lt = kp - k + 3;
     const uint32_t neg = V1[L] != 0u;
-    grp_mul<G, K>(g, P, Ptr{Z, k + 1}, k + 1, ResidualMag{V1, 2 * k - 1, L, lt, neg}, lt, s);
+    grp_mul<G, K, R>(g, P, Ptr{Z, k + 1}, k + 1, ResidualMag{V1, 2 * k - 1, L, lt, neg}, lt, s);
     Shifted zsh{Z, k + 1, 32 * (kp - k)};
     Shifted M{P, k + 1 + lt, -(32 * (k + 1) + 1)};
     if (neg) grp_sub<G>(g, Z2, zsh, M, kp + 1, 0u);
@@ -347,14 +347,14 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   }
   // S = floor(A * Z / 2^(32n + odd))   (n+1 limbs)
   const uint32_t ztop = Z[n];
-  grp_mulsq<G, K>(g, P, Ptr{sA, n}, Ptr{Z, n}, n, s);
+  grp_mulsq<G, K, R>(g, P, Ptr{sA, n}, Ptr{Z, n}, n, s);
   if (g.lane == 0) { P[2 * n] = 0; P[2 * n + 1] = 0; }
   g.sync();
   grp_add<G>(g, P + n, Ptr{P + n, n + 2}, SmallMul{sA, n, ztop}, n + 2, 0u);
   grp_copy<G>(g, S, Shifted{P, 2 * n + 2, -(32 * n + odd)}, n + 1);
-  // R = (A_ext - S^2) mod 2^(32(n+2)),  S = stop*2^(32n) + Slow
+  // Rm = (A_ext - S^2) mod 2^(32(n+2)),  S = stop*2^(32n) + Slow
   const uint32_t stop = S[n];
-  grp_mulsq<G, K>(g, V1, Ptr{S, n}, Ptr{S, n}, n, s);
+  grp_mulsq<G, K, R>(g, V1, Ptr{S, n}, Ptr{S, n}, n, s);
   if (g.lane == 0) { V1[2 * n] = 0; V1[2 * n + 1] = 0; V1[2 * n + 2] = 0; }
   g.sync();
   grp_add<G>(g, V1 + n, Ptr{V1 + n, n + 3}, SmallMul{S, n, 2u * stop}, n + 3, 0u);
@@ -362,28 +362,28 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
     const uint32_t ss = stop * stop;
     grp_add<G>(g, V1 + 2 * n, Ptr{V1 + 2 * n, 3}, Ptr{&ss, 1}, 3, 0u);
   }
-  grp_sub<G>(g, R, Ptr{X2, 2 * n}, Ptr{V1, 2 * n + 3}, n + 2, 0u);
-  // exact correction: 0 <= R <= 2S
+  grp_sub<G>(g, Rm, Ptr{X2, 2 * n}, Ptr{V1, 2 * n + 3}, n + 2, 0u);
+  // exact correction: 0 <= Rm <= 2S
   int guard = 0;
-  while ((R[n + 1] >> 31) != 0 && guard < 64) {       // R += 2S - 1, S -= 1
-    grp_add<G>(g, R, Ptr{R, n + 2}, ShlBits{S, n + 1, 1}, n + 2, 0u);
-    grp_sub<G>(g, R, Ptr{R, n + 2}, Zero{}, n + 2, 1u);
+  while ((Rm[n + 1] >> 31) != 0 && guard < 64) {       // Rm += 2S - 1, S -= 1
+    grp_add<G>(g, Rm, Ptr{Rm, n + 2}, ShlBits{S, n + 1, 1}, n + 2, 0u);
+    grp_sub<G>(g, Rm, Ptr{Rm, n + 2}, Zero{}, n + 2, 1u);
     grp_sub<G>(g, S, Ptr{S, n + 1}, Zero{}, n + 1, 1u);
     guard++;
   }
-  while (grp_cmp<G>(g, Ptr{R, n + 2}, ShlBits{S, n + 1, 1}, n + 2) > 0 && guard < 64) {   // R -= 2S + 1, S += 1
-    grp_sub<G>(g, R, Ptr{R, n + 2}, ShlBits{S, n + 1, 1}, n + 2, 1u);
+  while (grp_cmp<G>(g, Ptr{Rm, n + 2}, ShlBits{S, n + 1, 1}, n + 2) > 0 && guard < 64) {   // Rm -= 2S + 1, S += 1
+    grp_sub<G>(g, Rm, Ptr{Rm, n + 2}, ShlBits{S, n + 1, 1}, n + 2, 1u);
     grp_add<G>(g, S, Ptr{S, n + 1}, Zero{}, n + 1, 1u);
     guard++;
   }
   if (guard >= 64 && g.lane == 0) atomicOr(err, 2u);
-  const uint32_t rb = grp_cmp<G>(g, Ptr{R, n + 2}, Ptr{S, n + 1}, n + 2) > 0 ? 1u : 0u;
-  const uint32_t sticky = grp_is_zero<G>(g, Ptr{R, n + 2}, n + 2) ? 0u : 1u;
+  const uint32_t rb = grp_cmp<G>(g, Ptr{Rm, n + 2}, Ptr{S, n + 1}, n + 2) > 0 ? 1u : 0u;
+  const uint32_t sticky = grp_is_zero<G>(g, Ptr{Rm, n + 2}, n + 2) ? 0u : 1u;
   grp_add<G>(g, E, ShlBits{S, n + 1, 1}, Zero{}, n + 2, rb);
-  Rounded<G, K + 1> res;
-  grp_round<G, K + 1>(g, E, n + 2, n, sticky, mode, 0u, res);
+  Rounded res;
+  grp_round<G>(g, E, n + 2, n, sticky, mode, 0u, res);
   const long long er = h - 32LL * n - 1 + res.L + res.ovf;
-  write_value<G, K + 1>(g, r_exp, r, n, res, exp_word(er, 0u));
+  write_value<G>(g, r_exp, r, n, res, exp_word(er, 0u));
 }
 
 }  // namespace gfpa

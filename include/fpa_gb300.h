@@ -39,9 +39,10 @@ fpa_result fpa_copy_array_to_host_async(fpa_t fpa, uint32_t *exps, uint32_t *lim
 uint32_t fpa_gb300_device_errors(void);
 
 /* Lane-group configurations: configuration c runs one number per `lanes` threads with
- * product tiles of `tile_limbs` limbs and holds up to lanes*tile_limbs limbs. */
+ * product tiles of `tile_limbs` limbs, `pairs` column-block pairs per lane, and holds up
+ * to lanes*tile_limbs*pairs limbs. */
 int fpa_gb300_num_configs(void);
-fpa_result fpa_gb300_config_shape(int cfg, uint32_t *lanes, uint32_t *tile_limbs);
+fpa_result fpa_gb300_config_shape(int cfg, uint32_t *lanes, uint32_t *tile_limbs, uint32_t *pairs);
 /* choose the configuration used for numbers of `limbs` limbs (-1 = built-in default) */
 fpa_result fpa_gb300_set_config(uint32_t limbs, int cfg);
 int fpa_gb300_get_config(uint32_t limbs);
@@ -156,6 +157,13 @@ uint32_t fpa_batch_noalloc_errors(void *stream);
  * limbs (-1 = built-in default), settable per operation. */
 fpa_result fpa_gb300_set_op_config(fpa_op op, uint32_t limbs, int cfg);
 int fpa_gb300_get_op_config(fpa_op op, uint32_t limbs);
+/* Time every configuration that can hold `limbs` (and is at most 4x too large) on `sample`
+ * random operations of `op`, return the fastest and its rate (the table is not changed). */
+fpa_result fpa_gb300_autotune(fpa_op op, uint32_t limbs, uint32_t sample, int *best_cfg, double *ops_per_s);
+/* Load a table file of lines "op first_limbs last_limbs cfg" ('#' starts a comment).  The
+ * library loads tuned_configs.txt from the package directory (or the file named by the
+ * environment variable FPA_GB300_TUNING) when it is loaded. */
+fpa_result fpa_gb300_load_tuning(const char *path);
 
 /* Measured integer multiply-add throughput of the current GPU (mad.lo.u32 and mad.hi.u32
  * per second over all SMs): the roofline denominator for the multiply-bound operations. */

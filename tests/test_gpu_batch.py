@@ -112,15 +112,16 @@ def test_batch_rejects_bad_descriptors():
     empty.destroy()
 
 
-@pytest.mark.parametrize("cfg", range(10))
+@pytest.mark.parametrize("cfg", range(16))
 def test_every_configuration(cfg):
     """Force each lane-group configuration through the per-op table and check exactness
-    at a few sizes it can hold."""
-    lanes, tile = fpa.configs()[cfg]
-    cap = lanes * tile
+    at a few sizes it can hold (with several block pairs per lane: sizes that need one,
+    two and all of a lane's pairs)."""
+    lanes, tile, pairs = fpa.configs()[cfg]
+    cap = lanes * tile * pairs
     rng = np.random.default_rng(cfg)
-    for n in sorted({1, 3, cap // 2 + 1, cap - 1, cap} - {0}):
-        if n < 1 or n > 512:
+    for n in sorted({1, 3, lanes * tile + 1, cap // 2 + 1, cap - 1, cap} - {0}):
+        if n < 1 or n > min(cap, 512):
             continue
         ae, al = W.uniform(rng, 64, n, -200, 200)
         be, bl = W.uniform(rng, 64, n, -200, 200)
