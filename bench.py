@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--count", type=int, default=COUNT)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the 1024-bit, mixed-batch, chained and served measurements")
+    ap.add_argument("--quick-extras", action="store_true", help="smaller extra workloads")
     return ap.parse_args()
 
 
@@ -186,6 +189,204 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def hbm_peak():
+    """Measured copy bandwidth of this GPU model (GB/s) and where it came from."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (STREAM-style copy)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s (no measured copy bandwidth on this machine)"
+
+
+def _dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).cuda()
+
+
+def _timed(torch, fn, reps=3):
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def extra_add_mul_1024(fpa, torch, count=1 << 22):
+    """1024-bit add and mul (the 1024-bit workload's shape: uniform mantissas, e in [-64, 64],
+    random signs) over 2^22 pairs so that the operands (554 MB each) exceed L2; add is
+    HBM-bound, so its roofline is bytes moved per second against the copy bandwidth."""
+    from cubigfloat_gb300 import workloads as W
+    n = 32
+    (ae, al), (be, bl) = W.config1(11, count=count, n=n)
+    A, B, R = fpa.FpaArray(count, 32 * n), fpa.FpaArray(count, 32 * n), fpa.FpaArray(count, 32 * n)
+    A.to_device(ae, al)
+    B.to_device(be, bl)
+    out = {}
+    peak, src = hbm_peak()
+    for name, fn in (("add", fpa.fpa_add), ("mul", fpa.fpa_mul)):
+        ms = _timed(torch, lambda: fn(R, A, B, fpa.fpa_round_ties_to_even))
+        rec = {"ops_s": count / (ms / 1e3), "ms": ms}
+        if name == "add":
+            gbs = 3 * count * (4 + 4 * n) / (ms / 1e3) / 1e9
+            rec.update({"hbm_gbs": gbs, "hbm_peak_gbs": peak, "hbm_frac": gbs / peak, "peak_source": src})
+        out[name] = rec
+    del A, B, R
+    return {"workload": "1024-bit add and mul, 2^22 pairs, ties-to-even", **out}
+
+
+def extra_batched(fpa, torch, count):
+    """Mixed batch: `count` ops 30/20/30/10/10 add/sub/mul/div/sqrt, precision log-uniform in
+    256..16384 bits, one CUDA-graph launch of the persistent class kernels, against plain
+    per-(op, precision) elementwise launches over the same operands regrouped contiguously;
+    both results must be bit-identical."""
+    from cubigfloat_gb300 import workloads as W
+    descs, ae, al, be, bl, total = W.mixed(303, count)
+    d_ae, d_al, d_be, d_bl = (_dev(torch, x) for x in (ae, al, be, bl))
+    d_re = torch.zeros(count, dtype=torch.int32, device="cuda")
+    d_rl = torch.zeros(total, dtype=torch.int32, device="cuda")
+    b = fpa.Batch(descs)
+    ptrs = (d_re.data_ptr(), d_rl.data_ptr(), d_ae.data_ptr(), d_al.data_ptr(), d_be.data_ptr(), d_bl.data_ptr())
+    ms_run = _timed(torch, lambda: b.run(*ptrs))
+    assert b.capture(*ptrs) == 0
+    ms_graph = _timed(torch, lambda: b.graph_launch())
+    # plain: group (op, limbs) contiguously, one elementwise launch per group
+    order = np.lexsort((descs["limbs"], descs["op"]))
+    ops_s, lim_s = descs["op"][order], descs["limbs"][order]
+    starts = np.flatnonzero(np.r_[True, (ops_s[1:] != ops_s[:-1]) | (lim_s[1:] != lim_s[:-1])])
+    ends = np.r_[starts[1:], count]
+    lens = lim_s.astype(np.int64)
+    a_sel = np.repeat(descs["a_off"][order].astype(np.int64), lens) + (
+        np.arange(lens.sum()) - np.repeat(np.cumsum(lens) - lens, lens))
+    b_sel = np.repeat(descs["b_off"][order].astype(np.int64), lens) + (
+        np.arange(lens.sum()) - np.repeat(np.cumsum(lens) - lens, lens))
+    r_sel = np.repeat(descs["r_off"][order].astype(np.int64), lens) + (
+        np.arange(lens.sum()) - np.repeat(np.cumsum(lens) - lens, lens))
+    g_al, g_bl = _dev(torch, al[a_sel]), _dev(torch, bl[b_sel])
+    g_ae, g_be = _dev(torch, ae[order]), _dev(torch, be[order])
+    g_re = torch.zeros(count, dtype=torch.int32, device="cuda")
+    g_rl = torch.zeros(int(lens.sum()), dtype=torch.int32, device="cuda")
+    limb_pos = np.r_[0, np.cumsum(lens)]
+    groups = [(int(ops_s[s]), int(lim_s[s]), int(e - s), int(limb_pos[s]), int(s)) for s, e in zip(starts, ends)]
+
+    def plain():
+        for op, n, c, lo, eo in groups:
+            rc = fpa.elementwise(op, 32 * n, c, 3, g_re.data_ptr() + 4 * eo, g_rl.data_ptr() + 4 * lo,
+                                 g_ae.data_ptr() + 4 * eo, g_al.data_ptr() + 4 * lo, g_be.data_ptr() + 4 * eo,
+                                 g_bl.data_ptr() + 4 * lo)
+            assert rc == 0, rc
+    ms_plain = _timed(torch, plain)
+    re_b, rl_b = d_re.cpu().numpy(), d_rl.cpu().numpy()
+    re_p, rl_p = g_re.cpu().numpy(), g_rl.cpu().numpy()
+    same_e = np.array_equal(re_b[order], re_p)
+    valued = np.repeat(re_p > 8, lens)             # limbs are defined for ordinary values only
+    same_l = np.array_equal(rl_b[r_sel][valued], rl_p[valued])
+    tasks, _ = b.info()
+    b.destroy()
+    return {"workload": f"{count} mixed ops (add/sub/mul/div/sqrt 30/20/30/10/10), 256..16384 bits log-uniform",
+            "ops_s_graph": count / (ms_graph / 1e3), "ms_graph": ms_graph, "ms_run": ms_run,
+            "ops_s_plain_launches": count / (ms_plain / 1e3), "ms_plain": ms_plain, "plain_launches": len(groups),
+            "speedup_vs_plain": ms_plain / ms_graph, "tasks_per_class": tasks,
+            "bit_identical_to_plain": bool(same_e and same_l)}
+
+
+def extra_chains(fpa, torch, dots=10000, length=1024, newtons=10000):
+    """Dot products (acc += x*y, each step rounded, 2048 bits) and Newton sqrt
+    (y <- (y + x/y)/2, 8 iterations at 8192 bits, x in [1, 2)), one launch each."""
+    from cubigfloat_gb300 import workloads as W
+    rng = np.random.default_rng(4)
+    n = 64
+    xe, xl = W.uniform(rng, dots * length, n, -64, 64)
+    ye, yl = W.uniform(rng, dots * length, n, -64, 64)
+    dxe, dxl, dye, dyl = (_dev(torch, x) for x in (xe, xl, ye, yl))
+    del xl, yl
+    re_ = torch.zeros(dots, dtype=torch.int32, device="cuda")
+    rl = torch.zeros(dots * n, dtype=torch.int32, device="cuda")
+    ms_dot = _timed(torch, lambda: fpa.dot(2048, dots, length, 3, re_.data_ptr(), rl.data_ptr(), dxe.data_ptr(),
+                                           dxl.data_ptr(), dye.data_ptr(), dyl.data_ptr()), reps=2)
+    del dxe, dxl, dye, dyl
+    torch.cuda.empty_cache()
+    n2 = 256
+    xl2 = rng.integers(0, 1 << 32, size=(newtons, n2), dtype=np.uint64).astype(np.uint32)
+    xl2[:, -1] |= np.uint32(0x80000000)
+    xe2 = W.exp_word(np.ones(newtons, dtype=np.int64), 0)
+    y0 = np.zeros((newtons, n2), np.uint32)
+    y0[:, -1] = 0xC0000000
+    dxe2, dxl2 = _dev(torch, xe2), _dev(torch, xl2)
+    dye2, dyl2 = _dev(torch, xe2), _dev(torch, y0)
+    d_y0 = _dev(torch, y0)
+
+    def newton():
+        dyl2.copy_(d_y0)
+        dye2.copy_(dxe2)
+        assert fpa.newton_sqrt(8192, newtons, 8, 3, dye2.data_ptr(), dyl2.data_ptr(), dxe2.data_ptr(),
+                               dxl2.data_ptr()) == 0
+    ms_newton = _timed(torch, newton, reps=2)
+    return {"dot": {"workload": f"{dots} dot products of length {length} at 2048 bits",
+                    "ms": ms_dot, "mul_add_steps_s": dots * length / (ms_dot / 1e3)},
+            "newton_sqrt": {"workload": f"{newtons} Newton sqrt(x), 8 iterations at 8192 bits",
+                            "ms": ms_newton, "iterations_s": newtons * 8 / (ms_newton / 1e3)}}
+
+
+def extra_served(fpa, njobs=400, rates=(1000.0, 4000.0, None)):
+    """Served request stream: jobs of 1..4096 ops at one precision from {512, 1024, 4096,
+    16384} bits, Poisson arrivals at each rate (None = all jobs at once), through the
+    continuous-batching request loop and through plain per-job launches."""
+    from cubigfloat_gb300 import workloads as W
+    rng = np.random.default_rng(5)
+    jobs = [W.served_job(rng) for _ in range(njobs)]
+    total_ops = sum(len(j[1]) for j in jobs)
+    out = {"workload": f"{njobs} jobs, {total_ops} ops, sizes log-uniform 1..4096, op mix 30/20/30/10/10"}
+    for rate in rates:
+        arr = (W.poisson_arrivals(np.random.default_rng(int(rate or 0)), njobs, rate) if rate
+               else np.zeros(njobs))
+        rec = {}
+        for batching in (True, False):
+            srv = fpa.Server(hbm_budget_bytes=2 << 30, max_inflight=4, batching=batching)
+            ids = []
+            t0 = time.perf_counter()
+            for j, ta in zip(jobs, arr):
+                d = ta - (time.perf_counter() - t0)
+                if d > 0:
+                    time.sleep(d)
+                ids.append(srv.submit(*j)[0])
+            for i in ids:
+                assert srv.wait(i, 300000) == 0
+            tt = [srv.times(i) for i in ids]
+            lat = np.array([(t[2] - t[0]) / 1e6 for t in tt])
+            span = (max(t[2] for t in tt) - min(t[0] for t in tt)) / 1e9
+            st = srv.stats()
+            rec["batched" if batching else "plain"] = {
+                "ops_s": total_ops / span, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "batches": int(st["batches"]),
+                "peak_bytes": int(st["peak_bytes"])}
+            srv.destroy()
+        rec["throughput_vs_plain"] = rec["batched"]["ops_s"] / rec["plain"]["ops_s"]
+        out["burst" if rate is None else f"poisson_{int(rate)}_jobs_s"] = rec
+    return out
+
+
+def run_extras(fpa, torch, quick):
+    out = {}
+    for name, fn in (("add_mul_1024", lambda: extra_add_mul_1024(fpa, torch)),
+                     ("batched_mixed", lambda: extra_batched(fpa, torch, 100000 if quick else 1000000)),
+                     ("chains", lambda: extra_chains(fpa, torch, dots=1000 if quick else 10000,
+                                                     newtons=1000 if quick else 10000)),
+                     ("served", lambda: extra_served(fpa, njobs=100 if quick else 400))):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn()
+        except Exception as e:                      # reported, never hidden
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+        torch.cuda.empty_cache()
+    assert fpa.device_errors() == 0
+    return out
+
+
 def run_gb300(args):
     import torch
     rank, world, local = dist_env()
@@ -321,6 +522,9 @@ def run_gb300(args):
                 "per_op": {op: {"ms": round(per_op_ms[op], 3), "ops_s": round(count / (per_op_ms[op] / 1e3), 1),
                                 "imad_frac": round(2 * PRODUCTS[op] * count / (per_op_ms[op] / 1e3) / lo, 4)}
                            for op in OPS}}
+    extras = None
+    if not args.no_extras and world == 1:
+        extras = run_extras(fpa, torch, args.quick_extras)
     cpu = None
     if not args.no_cpu:
         cpu = cpu_leg(data, gpu_results, os.cpu_count() or 1)
@@ -337,7 +541,8 @@ def run_gb300(args):
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "e2e": {"value": e2e_val, "unit": "ops/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "api": "fpa_copy_array_to_device + fpa_mul/div/sqrt + fpa_copy_array_to_host (pinned)"},
-            "gpu_launches": len(OPS) * args.steps}
+            "gpu_launches": len(OPS) * args.steps,
+            "extras": extras}
     print(json.dumps(line))
     if world > 1:
         dist.barrier()

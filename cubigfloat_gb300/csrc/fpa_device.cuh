@@ -279,15 +279,17 @@ __device__ __forceinline__ void store_limbs(const Grp<G> &g, uint32_t *dst, int 
 //   sa   : N          operand x, zero padded to Mp*K
 //   sb   : N + 2K     operand y at offset K, K zero limbs below and above
 //   snap : G*3K       per-lane snapshot of the first block's column sums (reused per pair)
-//   part : 2GR*(K+2)  per-column-block partial sums (K+2 limbs each)
+//   ov   : 4GR        the two limbs above each column block's K limbs (2 per block)
+// A block's own K limbs go straight to the product buffer P; limbs at or above the product
+// length are never stored, so P needs room for the product only.
 template <int G, int K, int R>
 struct MulScratch {
   static_assert(G * R <= 32, "the block carry lookahead covers at most 64 column blocks");
   static constexpr int N = G * K * R;
-  uint32_t *sa, *sb, *snap, *part;
-  __host__ __device__ static constexpr int words() { return N + (N + 2 * K) + G * 3 * K + 2 * G * R * (K + 2); }
+  uint32_t *sa, *sb, *snap, *ov;
+  __host__ __device__ static constexpr int words() { return N + (N + 2 * K) + G * 3 * K + 4 * G * R; }
   __device__ __forceinline__ void carve(uint32_t *p) {
-    sa = p; sb = sa + N; snap = sb + N + 2 * K; part = snap + G * 3 * K;
+    sa = p; sb = sa + N; snap = sb + N + 2 * K; ov = snap + G * 3 * K;
   }
 };
 
@@ -315,6 +317,17 @@ __device__ __forceinline__ void columns_to_limbs(const uint32_t *lo, const uint3
 template <int G, int K, int R>
 __device__ __forceinline__ void blocks_final_sum_inl(const Grp<G> g, uint32_t *P, int outlen, int Mp,
                                                      const MulScratch<G, K, R> s);
+
+// A column block's K+2 limbs: the low K to P at K*cb (those below the product length), the
+// top two to ov[2cb..2cb+2).
+template <int K>
+__device__ __forceinline__ void emit_block(uint32_t *P, uint32_t *ov, int cb, int outlen, const uint32_t *L) {
+#pragma unroll
+  for (int j = 0; j < K; j++)
+    if (K * cb + j < outlen) P[K * cb + j] = L[j];
+  ov[2 * cb] = L[K];
+  ov[2 * cb + 1] = L[K + 1];
+}
 
 // Product P[0..lx+ly) of x (staged in s.sa, Mp = ceil(lx/K) blocks, zero padded) and y
 // (staged in s.sb at offset K, Mb = ceil(ly/K) <= Mp blocks, K zero limbs on each side).
@@ -386,16 +399,13 @@ __device__ __forceinline__ void grp_mul_staged(const Grp<G> g, uint32_t *P, int 
         asm("sub.cc.u32 %0, %0, %3;\n\tsubc.cc.u32 %1, %1, %4;\n\tsubc.u32 %2, %2, %5;"
             : "+r"(lo[c]), "+r"(hi[c]), "+r"(tp[c]) : "r"(a0), "r"(a1), "r"(a2));
       }
+      const int outlen = lx + ly;
       columns_to_limbs<K>(lo, hi, tp, L);
-      uint32_t *pp = s.part + (t + Mp) * (K + 2);
-#pragma unroll
-      for (int j = 0; j < K + 2; j++) pp[j] = L[j];
+      emit_block<K>(P, s.ov, t + Mp, outlen, L);
 #pragma unroll
       for (int c = 0; c < K; c++) { lo[c] = sn[c]; hi[c] = sn[K + c]; tp[c] = sn[2 * K + c]; }
       columns_to_limbs<K>(lo, hi, tp, L);
-      pp = s.part + t * (K + 2);
-#pragma unroll
-      for (int j = 0; j < K + 2; j++) pp[j] = L[j];
+      emit_block<K>(P, s.ov, t, outlen, L);
     }
   }
   g.sync();
@@ -432,9 +442,9 @@ __device__ __forceinline__ void grp_mul(const Grp<G> &g, uint32_t *P, X x, int l
   grp_mul_call<G, K, R>(g, P, la, lb, s);
 }
 
-// Sum of the per-block partials (K+2 limbs at block offsets K*cb) into P[0..outlen).
-// Each block cb = part[cb][0..K) + part[cb-1][K..K+2) is written without its carry in;
-// the carries between the 2*Mp <= 64 blocks come from one 64-bit lookahead over the
+// Sum of the per-block partials into P[0..outlen): block cb = its K limbs (already in P)
+// + the two limbs above block cb-1 (ov).  Each block is summed in place without its carry
+// in; the carries between the 2*Mp <= 64 blocks come from one 64-bit lookahead over the
 // generate / propagate ballots, and the (rare) blocks that receive one are incremented.
 template <int G, int K, int R>
 __device__ __forceinline__ void blocks_final_sum_inl(const Grp<G> g, uint32_t *P, int outlen, int Mp,
@@ -449,18 +459,18 @@ __device__ __forceinline__ void blocks_final_sum_inl(const Grp<G> g, uint32_t *P
       const int cb = t + half * Mp;
       uint32_t gen = 0, prop = 0;
       if (t < Mp) {
-        const uint32_t *pc = s.part + cb * (K + 2);
         uint32_t c0 = 0, c1 = 0;
-        if (cb > 0) { c0 = s.part[(cb - 1) * (K + 2) + K]; c1 = s.part[(cb - 1) * (K + 2) + K + 1]; }
+        if (cb > 0) { c0 = s.ov[2 * (cb - 1)]; c1 = s.ov[2 * (cb - 1) + 1]; }
         uint64_t carry = 0;
         uint32_t all1 = 1u;
 #pragma unroll
         for (int j = 0; j < K; j++) {
-          const uint64_t sum = (uint64_t)pc[j] + carry + (j == 0 ? c0 : 0u) + (j == 1 ? c1 : 0u);
+          const int idx = K * cb + j;
+          const uint32_t pv = idx < outlen ? P[idx] : 0u;
+          const uint64_t sum = (uint64_t)pv + carry + (j == 0 ? c0 : 0u) + (j == 1 ? c1 : 0u);
           const uint32_t v = (uint32_t)sum;
           carry = sum >> 32;
           all1 &= (v == 0xFFFFFFFFu);
-          const int idx = K * cb + j;
           if (idx < outlen) P[idx] = v;
         }
         gen = (uint32_t)(carry != 0);

@@ -129,25 +129,31 @@ __global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(Elemen
 template <int OP>
 static cudaError_t launch_op(const ElementwiseArgs &args, cudaStream_t stream, int sms) {
   constexpr int G = CFG_G, K = CFG_K, R = CFG_R;
-  // four warps per CTA, fewer when one warp's groups need more than a quarter of the
-  // 227 KB a CTA may use
   constexpr size_t warp_bytes = (size_t)(32 / G) * Words<OP, G, K, R>::aligned() * sizeof(uint32_t);
   constexpr size_t cta_max = 227 * 1024;
   if constexpr (warp_bytes > cta_max) return cudaErrorInvalidConfiguration;
-  constexpr int warps = warp_bytes * 4 <= cta_max ? 4 : (warp_bytes * 2 <= cta_max ? 2 : 1);
-  constexpr int threads = 32 * warps;
-  constexpr int gpc = threads / G;
-  const size_t smem = (size_t)warps * warp_bytes;
-  static int configured = 0, per_sm = 1;
+  // CTA of 4, 2 or 1 warps, whichever keeps the most warps resident on an SM: shared memory
+  // is granted per CTA, so where four warps' worth does not fit once more, a smaller CTA
+  // may still fit.
+  static int configured = 0, warps = 1, per_sm = 1;
   auto kern = k_elementwise<OP, G, K, R>;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int wmax = warp_bytes * 4 <= cta_max ? 4 : (warp_bytes * 2 <= cta_max ? 2 : 1);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(wmax * warp_bytes));
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
-    if (e != cudaSuccess) return e;
+    int best = 0;
+    for (int w = wmax; w >= 1; w >>= 1) {
+      int blocks = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, 32 * w, w * warp_bytes);
+      if (e != cudaSuccess) return e;
+      if (blocks * w > best) { best = blocks * w; warps = w; per_sm = blocks; }
+    }
     if (per_sm < 1) per_sm = 1;
     configured = 1;
   }
+  const int threads = 32 * warps, gpc = threads / G;
+  const size_t smem = (size_t)warps * warp_bytes;
   const uint64_t need = (args.count + gpc - 1) / gpc;
   const uint64_t cap = (uint64_t)sms * (uint64_t)per_sm;
   const unsigned grid = (unsigned)(need < cap ? need : cap);

@@ -16,8 +16,8 @@ struct OpSpace {
   static constexpr int N = G * K * R;
   __host__ __device__ static constexpr int addsub() { return 3 * N + 8; }
   __host__ __device__ static constexpr int mul() { return 2 * N + 4; }
-  __host__ __device__ static constexpr int div() { return 2 * N + (N + 4) * 2 + (2 * N + 8) * 2 + (N + 8) * 3; }
-  __host__ __device__ static constexpr int sqrt() { return N + (2 * N + 4) + (N + 4) * 2 + (2 * N + 8) * 5 + (N + 8) * 2; }
+  __host__ __device__ static constexpr int div() { return (N + 4) * 2 + (2 * N + 8) * 2 + (N + 8); }
+  __host__ __device__ static constexpr int sqrt() { return (N + 4) * 3 + (N + 8) * 4 + (2 * N + 8); }
   __host__ __device__ static constexpr int max_all() {
     int a = addsub(), b = mul(), c = div(), d = sqrt();
     int m = a > b ? a : b; m = m > c ? m : c; m = m > d ? m : d;
@@ -208,11 +208,12 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   const uint32_t act = c_action[3][classify(a_exp) * 9 + classify(b_exp)];
   if (act != ACT_DIV) { write_class<G>(g, r_exp, act); return; }
   MulScratch<G, K, R> s; s.carve(ws);
-  uint32_t *sA = ws + MulScratch<G, K, R>::words(), *sB = sA + N;
-  uint32_t *Y = sB + N, *Y2 = Y + (N + 4);
+  // the operands are read where they lie (a, b): only the quotient's state is staged
+  uint32_t *Y = ws + MulScratch<G, K, R>::words(), *Y2 = Y + (N + 4);
   uint32_t *T = Y2 + (N + 4), *P2 = T + (2 * N + 8);
-  uint32_t *Q = P2 + (2 * N + 8), *Rm = Q + (N + 8), *X = Rm + (N + 8);
-  for (int i = g.lane; i < n; i += G) { sA[i] = a[i]; sB[i] = b[i]; }
+  uint32_t *Q = P2 + (2 * N + 8);
+  uint32_t *Rm = T;                  // T (A*Y) is dead once Q is copied out of it
+  uint32_t *X = P2;                  // P2 (Q*B) is dead once Rm is formed
   if (g.lane == 0) {
     uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)b[n - 1];   // level 1: floor((2^64-1)/B_top)
     Y[0] = (uint32_t)y; Y[1] = (uint32_t)(y >> 32);
@@ -222,7 +223,7 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   const int nl = newton_levels(n, lv);
   for (int li = 1; li < nl; li++) {
     const int k = lv[li - 1], kp = lv[li];
-    const uint32_t *Bk = sB + (n - kp);
+    const uint32_t *Bk = b + (n - kp);
     // T = B_k' * Y_k   (k' x (k+1) limbs)
     grp_mul<G, K, R>(g, T, Ptr{Bk, kp}, kp, Ptr{Y, k + 1}, k + 1, s);
     // M = (Y_k * (|E| >> 32(k-1))) >> 32(k+1)
@@ -238,32 +239,32 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   }
   // Q = floor(A * Y / 2^(32n)),  n+1 limbs;  Y = ytop*2^(32n) + Ylow
   const uint32_t ytop = Y[n];
-  grp_mulsq<G, K, R>(g, T, Ptr{sA, n}, Ptr{Y, n}, n, s);
+  grp_mulsq<G, K, R>(g, T, Ptr{a, n}, Ptr{Y, n}, n, s);
   if (g.lane == 0) { T[2 * n] = 0; T[2 * n + 1] = 0; }
   g.sync();
-  grp_add<G>(g, T + n, Ptr{T + n, n + 2}, SmallMul{sA, n, ytop}, n + 2, 0u);
+  grp_add<G>(g, T + n, Ptr{T + n, n + 2}, SmallMul{a, n, ytop}, n + 2, 0u);
   grp_copy<G>(g, Q, Ptr{T + n, n + 2}, n + 1);
   // Rm = (A * 2^(32n) - Q * B) mod 2^(32(n+2))
   const uint32_t qtop = Q[n];
-  grp_mulsq<G, K, R>(g, P2, Ptr{Q, n}, Ptr{sB, n}, n, s);
+  grp_mulsq<G, K, R>(g, P2, Ptr{Q, n}, Ptr{b, n}, n, s);
   if (g.lane == 0) { P2[2 * n] = 0; P2[2 * n + 1] = 0; P2[2 * n + 2] = 0; }
   g.sync();
-  grp_add<G>(g, P2 + n, Ptr{P2 + n, n + 3}, SmallMul{sB, n, qtop}, n + 3, 0u);
-  grp_sub<G>(g, Rm, Shifted{sA, n, 32 * n}, Ptr{P2, 2 * n + 3}, n + 2, 0u);
+  grp_add<G>(g, P2 + n, Ptr{P2 + n, n + 3}, SmallMul{b, n, qtop}, n + 3, 0u);
+  grp_sub<G>(g, Rm, Shifted{a, n, 32 * n}, Ptr{P2, 2 * n + 3}, n + 2, 0u);
   // exact correction: 0 <= Rm < B
   int guard = 0;
   while ((Rm[n + 1] >> 31) != 0 && guard < 64) {
     grp_sub<G>(g, Q, Ptr{Q, n + 1}, Zero{}, n + 1, 1u);
-    grp_add<G>(g, Rm, Ptr{Rm, n + 2}, Ptr{sB, n}, n + 2, 0u);
+    grp_add<G>(g, Rm, Ptr{Rm, n + 2}, Ptr{b, n}, n + 2, 0u);
     guard++;
   }
-  while (grp_cmp<G>(g, Ptr{Rm, n + 2}, Ptr{sB, n}, n + 2) >= 0 && guard < 64) {
+  while (grp_cmp<G>(g, Ptr{Rm, n + 2}, Ptr{b, n}, n + 2) >= 0 && guard < 64) {
     grp_add<G>(g, Q, Ptr{Q, n + 1}, Zero{}, n + 1, 1u);
-    grp_sub<G>(g, Rm, Ptr{Rm, n + 2}, Ptr{sB, n}, n + 2, 0u);
+    grp_sub<G>(g, Rm, Ptr{Rm, n + 2}, Ptr{b, n}, n + 2, 0u);
     guard++;
   }
   if (guard >= 64 && g.lane == 0) atomicOr(err, 1u);
-  const int c2 = grp_cmp<G>(g, ShlBits{Rm, n + 2, 1}, Ptr{sB, n}, n + 2);
+  const int c2 = grp_cmp<G>(g, ShlBits{Rm, n + 2, 1}, Ptr{b, n}, n + 2);
   const uint32_t rb = c2 >= 0 ? 1u : 0u;
   const uint32_t sticky = (!grp_is_zero<G>(g, Ptr{Rm, n + 2}, n + 2) && c2 != 0) ? 1u : 0u;
   // X = 2Q + rb  (n+2 limbs)
@@ -304,19 +305,20 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   const uint32_t act = c_sqrt_action[classify(a_exp)];
   if (act != ACT_SQRT) { write_class<G>(g, r_exp, act); return; }
   MulScratch<G, K, R> s; s.carve(ws);
-  uint32_t *sA = ws + MulScratch<G, K, R>::words();
-  uint32_t *X2 = sA + N;                       // A_ext, 2n limbs
-  uint32_t *Z = X2 + (2 * N + 4), *Z2 = Z + (N + 4);
-  uint32_t *W = Z2 + (N + 4), *V1 = W + (2 * N + 8), *V2 = V1 + (2 * N + 8), *P = V2 + (2 * N + 8);
-  uint32_t *E = P + (2 * N + 8), *S = E + (2 * N + 8), *Rm = S + (N + 8);
+  // A_ext = A * 2^(32n - odd) has 2n limbs of which the low n-1 are zero: only its top n+1
+  // limbs Xh = A * 2^(32 - odd) are kept (A_ext limb i = Xh[i - (n-1)]).
+  uint32_t *Xh = ws + MulScratch<G, K, R>::words();
+  uint32_t *Z = Xh + (N + 4), *Z2 = Z + (N + 4);
+  uint32_t *W = Z2 + (N + 4);        // Z_k^2: 2k+2 <= n+4 limbs
+  uint32_t *V1 = W + (N + 8), *V2 = V1 + (2 * N + 8), *P = V2 + (N + 8), *S = P + (N + 8);
+  uint32_t *Rm = V2;                 // V2 (kp + 2k+2-kp <= n+4 limbs) is dead after the Newton loop
+  uint32_t *E = W;                   // W (Z^2) is dead after the Newton loop
   const long long e = (long long)(a_exp >> 1) - BIAS;
   const int odd = (int)(e & 1);
   const long long h = (e + odd) / 2;           // exact: e + odd is even
-  for (int i = g.lane; i < n; i += G) sA[i] = a[i];
-  g.sync();
-  grp_copy<G>(g, X2, Shifted{sA, n, 32 * n - odd}, 2 * n);
+  grp_copy<G>(g, Xh, Shifted{a, n, 32 - odd}, n + 1);
   if (g.lane == 0) {
-    uint64_t x1 = (uint64_t)X2[2 * n - 1] << 32;         // top limb of A_ext, in [2^30, 2^32)
+    uint64_t x1 = (uint64_t)Xh[n] << 32;                   // top limb of A_ext, in [2^30, 2^32)
     uint64_t s1 = isqrt64(x1);                             // in [2^31, 2^32)
     uint64_t z = 0xFFFFFFFFFFFFFFFFull / s1;               // level 1: ~ 2^32 / sqrt(x)
     Z[0] = (uint32_t)z; Z[1] = (uint32_t)(z >> 32);
@@ -329,7 +331,7 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
     // W = Z_k^2  (Z_k has k+1 limbs)
     grp_mulsq<G, K, R>(g, W, Ptr{Z, k + 1}, Ptr{Z, k + 1}, k + 1, s);
     // V = X_k' * W = X*W[0..k') + (X*W[k'..2k+2)) << k'   (the second factor is short)
-    const uint32_t *Xk = X2 + (2 * n - kp);
+    const uint32_t *Xk = Xh + (n + 1 - kp);             // top k' limbs of A_ext (k' <= n)
     const int ls = 2 * k + 2 - kp;
     grp_mulsq<G, K, R>(g, V1, Ptr{Xk, kp}, Ptr{W, kp}, kp, s);
     grp_mul<G, K, R>(g, V2, Ptr{Xk, kp}, kp, Ptr{W + kp, ls}, ls, s);
@@ -347,11 +349,11 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   }
   // S = floor(A * Z / 2^(32n + odd))   (n+1 limbs)
   const uint32_t ztop = Z[n];
-  grp_mulsq<G, K, R>(g, P, Ptr{sA, n}, Ptr{Z, n}, n, s);
-  if (g.lane == 0) { P[2 * n] = 0; P[2 * n + 1] = 0; }
+  grp_mulsq<G, K, R>(g, V1, Ptr{a, n}, Ptr{Z, n}, n, s);
+  if (g.lane == 0) { V1[2 * n] = 0; V1[2 * n + 1] = 0; }
   g.sync();
-  grp_add<G>(g, P + n, Ptr{P + n, n + 2}, SmallMul{sA, n, ztop}, n + 2, 0u);
-  grp_copy<G>(g, S, Shifted{P, 2 * n + 2, -(32 * n + odd)}, n + 1);
+  grp_add<G>(g, V1 + n, Ptr{V1 + n, n + 2}, SmallMul{a, n, ztop}, n + 2, 0u);
+  grp_copy<G>(g, S, Shifted{V1, 2 * n + 2, -(32 * n + odd)}, n + 1);
   // Rm = (A_ext - S^2) mod 2^(32(n+2)),  S = stop*2^(32n) + Slow
   const uint32_t stop = S[n];
   grp_mulsq<G, K, R>(g, V1, Ptr{S, n}, Ptr{S, n}, n, s);
@@ -362,7 +364,7 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
     const uint32_t ss = stop * stop;
     grp_add<G>(g, V1 + 2 * n, Ptr{V1 + 2 * n, 3}, Ptr{&ss, 1}, 3, 0u);
   }
-  grp_sub<G>(g, Rm, Ptr{X2, 2 * n}, Ptr{V1, 2 * n + 3}, n + 2, 0u);
+  grp_sub<G>(g, Rm, Shifted{Xh, n + 1, 32 * (n - 1)}, Ptr{V1, 2 * n + 3}, n + 2, 0u);
   // exact correction: 0 <= Rm <= 2S
   int guard = 0;
   while ((Rm[n + 1] >> 31) != 0 && guard < 64) {       // Rm += 2S - 1, S -= 1
