@@ -47,7 +47,7 @@ static bool cfg_fits(int c, uint32_t n) {
 int gfpa_cfg_for_op(int op, uint32_t n) {
   if (op < 0 || op > 4 || n == 0 || n > GFPA_MAX_LIMBS) return -1;
   const int c = g_state.cfg_override[op][n] - 1;
-  if (c >= 0 && cfg_fits(c, n)) return c;
+  if (c >= 0 && cfg_fits(c, n) && gfpa_cfg_supports(c, op)) return c;
   return gfpa_default_cfg(n < 4 ? 4 : n);
 }
 
@@ -280,6 +280,7 @@ fpa_result fpa_gb300_set_op_config(fpa_op op, uint32_t limbs, int cfg) {
   if (limbs == 0 || limbs > GFPA_MAX_LIMBS) return fpa_invalid_precisions;
   if (cfg < -1 || cfg >= GFPA_NUM_CFGS) return fpa_math_error;
   if (cfg >= 0 && !cfg_fits(cfg, limbs)) return fpa_invalid_precisions;
+  if (cfg >= 0 && !gfpa_cfg_supports(cfg, (int)op)) return fpa_math_error;
   std::lock_guard<std::mutex> lk(g_state.mu);
   g_state.cfg_override[(int)op][limbs] = (int8_t)(cfg + 1);
   return fpa_success;
@@ -289,6 +290,7 @@ int fpa_gb300_get_op_config(fpa_op op, uint32_t limbs) { return gfpa_cfg_for_op(
 
 fpa_result fpa_gb300_set_config(uint32_t limbs, int cfg) {
   for (int op = 0; op < 5; op++) {
+    if (cfg >= 0 && !gfpa_cfg_supports(cfg, op)) continue;      // add/sub-only configuration
     fpa_result r = fpa_gb300_set_op_config((fpa_op)op, limbs, cfg);
     if (r != fpa_success) return r;
   }

@@ -70,6 +70,18 @@ cudaError_t launch(int c, const BatchArgs *a, int grid, size_t smem, cudaStream_
 }  // namespace
 
 int gfpa_batch_warp_words(int cfg, int op) { return warp_words_for(cfg, op); }
+
+int gfpa_batch_cfg_for(int op, uint32_t n) {
+  const int cfg = gfpa_cfg_for_op(op, n);
+  if (cfg < 0) return cfg;
+  // one-thread configurations have their own elementwise kernel only, and a chosen
+  // configuration whose warps need more shared memory than one CTA of its class can hold
+  // gives way to the default one
+  if (gfpa_cfg_G[cfg] == 1 || (size_t)(gfpa_class_threads[gfpa_class_of(cfg, op)] / 32) * warp_words_for(cfg, op) * 4 >
+                                  227 * 1024)
+    return gfpa_default_cfg(n < 4 ? 4 : n);
+  return cfg;
+}
 double gfpa_batch_op_weight(int op, int n) { return op_weight(op, n); }
 cudaError_t gfpa_batch_prepare_class(int c, size_t smem, int *per_sm) { return prepare(c, smem, per_sm); }
 cudaError_t gfpa_batch_launch_class(int c, const BatchArgs *a, int grid, size_t smem, cudaStream_t st) {
@@ -87,12 +99,8 @@ fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms,
     const fpa_batch_desc &d = descs[i];
     if (d.op > 4 || d.mode > 4) return fpa_math_error;
     if (d.limbs == 0 || d.limbs > GFPA_MAX_LIMBS) return fpa_invalid_precisions;
-    int cfg = gfpa_cfg_for_op(d.op, d.limbs);
+    const int cfg = gfpa_batch_cfg_for(d.op, d.limbs);
     if (cfg < 0) return fpa_invalid_precisions;
-    // a chosen configuration whose warps need more shared memory than one CTA of its class
-    // can hold gives way to the default one
-    if ((size_t)(gfpa_class_threads[gfpa_class_of(cfg, d.op)] / 32) * warp_words_for(cfg, d.op) * 4 > 227 * 1024)
-      cfg = gfpa_default_cfg(d.limbs < 4 ? 4 : d.limbs);
     key[i] = (uint16_t)(cfg * 5 + d.op);
     cls[i] = (uint8_t)gfpa_class_of(cfg, d.op);
     order[i] = (uint32_t)i;

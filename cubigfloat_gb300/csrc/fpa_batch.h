@@ -68,6 +68,7 @@ cudaError_t gfpa_batch_enqueue(const BatchPlan &plan, const fpa_batch_desc *d_de
 
 // Planner helpers shared with other entry points of the batched form.
 int gfpa_batch_warp_words(int cfg, int op);          // shared-memory words per warp
+int gfpa_batch_cfg_for(int op, uint32_t n);           // configuration a batch task runs with
 double gfpa_batch_op_weight(int op, int n);           // relative cost of one operation
 cudaError_t gfpa_batch_prepare_class(int c, size_t smem, int *blocks_per_sm);
 cudaError_t gfpa_batch_launch_class(int c, const BatchArgs *a, int grid, size_t smem, cudaStream_t st);

@@ -74,7 +74,7 @@ extern "C" fpa_result fpa_batch_run_noalloc(const fpa_batch_desc *descs, uint32_
     const fpa_batch_desc &d = descs[i];
     if (d.op > 4 || d.mode > 4) return fpa_math_error;
     if (d.limbs == 0 || d.limbs > GFPA_MAX_LIMBS) return fpa_invalid_precisions;
-    const int cfg = gfpa_cfg_for_op(d.op, d.limbs);
+    const int cfg = gfpa_batch_cfg_for(d.op, d.limbs);
     if (cfg < 0) return fpa_invalid_precisions;
     h_key[i] = (uint16_t)(cfg * 5 + d.op);
     h_cls[i] = (uint8_t)gfpa_class_of(cfg, d.op);

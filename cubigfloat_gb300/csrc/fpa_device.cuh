@@ -216,6 +216,33 @@ __device__ __forceinline__ void grp_copy(const Grp<G> &g, uint32_t *dst, X x, in
 __device__ __forceinline__ uint32_t clz32(uint32_t v) { return (uint32_t)__clz((int)v); }
 
 // ---------------------------------------------------------------------------------------
+// Asynchronous global -> shared copies (cp.async): add/sub stage the next operation's
+// operands while they compute the current one, so loads stay in flight.
+__device__ __forceinline__ void cp_async4(uint32_t *dst, const uint32_t *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(uint32_t *dst, const uint32_t *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+               "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// wait until at most PENDING of this thread's committed groups are still in flight
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory"); }
+
+// the group copies n limbs src -> dst asynchronously; vec: 16-byte pieces (n % 4 == 0 and
+// both addresses 16-byte aligned)
+template <int G>
+__device__ __forceinline__ void grp_stage_async(const Grp<G> &g, uint32_t *dst, const uint32_t *src, int n, bool vec) {
+  if (vec) {
+    for (int c = g.lane; c < (n >> 2); c += G) cp_async16(dst + 4 * c, src + 4 * c);
+  } else {
+    for (int i = g.lane; i < n; i += G) cp_async4(dst + i, src + i);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // Rounding of a nonnegative integer X[0..xlen) (shared memory) to n limbs.
 // grp_round decides the rounding (group-uniform); store_limbs then writes the rounded
 // limbs straight from X, so X must stay unchanged until the store.  Returns false when
@@ -418,15 +445,16 @@ __device__ __forceinline__ void grp_mulsq_staged(const Grp<G> g, uint32_t *P, in
   grp_mul_staged<G, K, R>(g, P, m, m, s);
 }
 
-// Out-of-line copy of the product for the operations that call it many times (div, sqrt):
-// one copy of the unrolled tile loop keeps their code inside the instruction cache.
+
+// P[0..lx+ly) = x[0..lx) * y[0..ly) for functor operands (lx, ly <= G*K*R, any order): the
+// longer one is staged as the block operand.
+// Out-of-line product core for the operations that call it many times (div, sqrt): one
+// copy of the unrolled tile loop keeps their code inside the instruction cache.
 template <int G, int K, int R>
 __device__ __noinline__ void grp_mul_call(const Grp<G> g, uint32_t *P, int lx, int ly, const MulScratch<G, K, R> s) {
   grp_mul_staged<G, K, R>(g, P, lx, ly, s);
 }
 
-// P[0..lx+ly) = x[0..lx) * y[0..ly) for functor operands (lx, ly <= G*K*R, any order): the
-// longer one is staged as the block operand.
 template <int G, int K, int R, class X, class Y>
 __device__ __forceinline__ void grp_mul(const Grp<G> &g, uint32_t *P, X x, int lx, Y y, int ly,
                                         const MulScratch<G, K, R> &s) {

@@ -100,6 +100,89 @@ struct MinBlocks {
                            : ((OP == OP_DIV || OP == OP_SQRT) ? (K >= 8 ? 4 : GFPA_NEWTON_MINBLOCKS) : (K >= 8 ? 4 : 8));
 };
 
+// add/sub: HBM-bound, so each group double-buffers its operands: the copies of its next
+// operation (cp.async) are in flight while it computes the current one.
+template <int OP, int G, int K, int R>
+__device__ __forceinline__ void addsub_pipelined(const Grp<G> &g, uint32_t *ws, const ElementwiseArgs &args,
+                                                 uint64_t i, uint64_t stride) {
+  constexpr int N = G * K * R;
+  const int n = (int)args.n;
+  uint32_t *X = ws + 4 * N;
+  const bool vec = (n & 3) == 0 && ((((uintptr_t)args.a_limbs) | ((uintptr_t)args.b_limbs)) & 15) == 0;
+  uint32_t ae = 0, be = 0;
+  if (i < args.count) {
+    grp_stage_async<G>(g, ws, args.a_limbs + i * n, n, vec);
+    grp_stage_async<G>(g, ws + N, args.b_limbs + i * n, n, vec);
+    ae = args.a_exps[i]; be = args.b_exps[i];
+  }
+  cp_async_commit();
+  int cur = 0;
+  for (; i < args.count; i += stride) {
+    const uint64_t nx = i + stride;
+    uint32_t nae = 0, nbe = 0;
+    if (nx < args.count) {
+      uint32_t *nb = ws + (cur ^ 1) * 2 * N;
+      grp_stage_async<G>(g, nb, args.a_limbs + nx * n, n, vec);
+      grp_stage_async<G>(g, nb + N, args.b_limbs + nx * n, n, vec);
+      nae = args.a_exps[nx]; nbe = args.b_exps[nx];
+    }
+    cp_async_commit();
+    cp_async_wait<1>();                          // this operation's operands have landed
+    g.sync();
+    const uint32_t *sa = ws + cur * 2 * N;
+    op_addsub_staged<G>(g, X, n, args.mode, OP == OP_SUB, ae, sa, be, sa + N, args.r_exps + i,
+                        args.r_limbs + i * n);
+    g.sync();                                    // the buffer is refilled two operations on
+    ae = nae; be = nbe; cur ^= 1;
+  }
+  cp_async_wait<0>();
+}
+
+// mul: the same double buffering; the zero padding around the staged operands is the same
+// for every operation of a launch, so it is written once.
+template <int G, int K, int R>
+__device__ __forceinline__ void mul_pipelined(const Grp<G> &g, uint32_t *ws, const ElementwiseArgs &args, uint64_t i,
+                                              uint64_t stride) {
+  constexpr int N = G * K * R;
+  const int n = (int)args.n;
+  const int NK = ((n + K - 1) / K) * K;
+  MulScratch<G, K, R> s; s.carve(ws);
+  uint32_t *P = ws + MulScratch<G, K, R>::words();
+  uint32_t *xa[2] = {s.sa, P + 2 * N + 4};
+  uint32_t *yb[2] = {s.sb, xa[1] + N};
+  for (int j = g.lane; j < NK; j += G)
+    if (j >= n) { xa[0][j] = 0u; xa[1][j] = 0u; }
+  for (int j = g.lane; j < NK + 2 * K; j += G)
+    if (j < K || j >= K + n) { yb[0][j] = 0u; yb[1][j] = 0u; }
+  const bool va = (n & 3) == 0 && (((uintptr_t)args.a_limbs) & 15) == 0;
+  const bool vb = va && (K & 3) == 0 && (((uintptr_t)args.b_limbs) & 15) == 0;
+  uint32_t ae = 0, be = 0;
+  if (i < args.count) {
+    grp_stage_async<G>(g, xa[0], args.a_limbs + i * n, n, va);
+    grp_stage_async<G>(g, yb[0] + K, args.b_limbs + i * n, n, vb);
+    ae = args.a_exps[i]; be = args.b_exps[i];
+  }
+  cp_async_commit();
+  int cur = 0;
+  for (; i < args.count; i += stride) {
+    const uint64_t nx = i + stride;
+    uint32_t nae = 0, nbe = 0;
+    if (nx < args.count) {
+      grp_stage_async<G>(g, xa[cur ^ 1], args.a_limbs + nx * n, n, va);
+      grp_stage_async<G>(g, yb[cur ^ 1] + K, args.b_limbs + nx * n, n, vb);
+      nae = args.a_exps[nx]; nbe = args.b_exps[nx];
+    }
+    cp_async_commit();
+    cp_async_wait<1>();                          // this operation's operands have landed
+    g.sync();
+    s.sa = xa[cur]; s.sb = yb[cur];
+    op_mul_staged<G, K, R>(g, s, P, n, args.mode, ae, be, args.r_exps + i, args.r_limbs + i * n);
+    g.sync();                                    // the buffer is refilled two operations on
+    ae = nae; be = nbe; cur ^= 1;
+  }
+  cp_async_wait<0>();
+}
+
 template <int OP, int G, int K, int R>
 __global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(ElementwiseArgs args) {
   extern __shared__ __align__(16) uint32_t smem[];
@@ -107,6 +190,14 @@ __global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(Elemen
   const uint32_t gpc = blockDim.x / G, gi = threadIdx.x / G;
   uint32_t *ws = smem + gi * Words<OP, G, K, R>::aligned();
   const int n = (int)args.n;
+  if constexpr (OP == OP_ADD || OP == OP_SUB) {
+    addsub_pipelined<OP, G, K, R>(g, ws, args, (uint64_t)blockIdx.x * gpc + gi, (uint64_t)gridDim.x * gpc);
+    return;
+  }
+  if constexpr (OP == OP_MUL) {
+    mul_pipelined<G, K, R>(g, ws, args, (uint64_t)blockIdx.x * gpc + gi, (uint64_t)gridDim.x * gpc);
+    return;
+  }
   for (uint64_t i = (uint64_t)blockIdx.x * gpc + gi; i < args.count; i += (uint64_t)gridDim.x * gpc) {
     const uint64_t off = i * (uint64_t)n;
     const uint32_t a_exp = args.a_exps[i];

@@ -17,18 +17,21 @@ struct ElementwiseArgs {
   uint32_t *err;
 };
 
-#define GFPA_NUM_CFGS 16
+#define GFPA_NUM_CFGS 18
 #define GFPA_NUM_DEFAULT_CFGS 7
 #define GFPA_MAX_LIMBS 512
 
 // Lane-group configurations (G lanes x K limbs per tile x R block pairs per lane, capacity
 // G*K*R limbs).  0..6 are the defaults in increasing capacity; 7..15 put two to eight
 // operations in one warp (fewer lanes per operation, wider tiles or several block pairs
-// per lane), which the autotuner can choose (mostly for div/sqrt).
-static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4};
-static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4};
-static const int gfpa_cfg_R[GFPA_NUM_CFGS] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 2, 4, 2, 8};
+// per lane), which the autotuner can choose (mostly for div/sqrt); 16 and 17 run add/sub
+// with one thread per operation (capacity 32 and 64 limbs; fpa_thread_kernels.cu).
+static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4, 1, 1};
+static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4, 32, 64};
+static const int gfpa_cfg_R[GFPA_NUM_CFGS] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 2, 4, 2, 8, 1, 1};
 static inline int gfpa_cfg_capacity(int c) { return gfpa_cfg_G[c] * gfpa_cfg_K[c] * gfpa_cfg_R[c]; }
+// operations a configuration runs (the one-thread configurations run add/sub only)
+static inline bool gfpa_cfg_supports(int c, int op) { return gfpa_cfg_G[c] > 1 || op <= 1; }
 
 extern "C" {
 cudaError_t gfpa_launch_cfg0(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
@@ -47,6 +50,8 @@ cudaError_t gfpa_launch_cfg12(int op, const ElementwiseArgs *args, cudaStream_t 
 cudaError_t gfpa_launch_cfg13(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 cudaError_t gfpa_launch_cfg14(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 cudaError_t gfpa_launch_cfg15(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg16(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg17(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 }
 
 // smallest default configuration whose capacity holds n limbs
@@ -74,6 +79,8 @@ static inline cudaError_t gfpa_launch(int cfg, int op, const ElementwiseArgs *ar
     case 13: return gfpa_launch_cfg13(op, args, stream, sms);
     case 14: return gfpa_launch_cfg14(op, args, stream, sms);
     case 15: return gfpa_launch_cfg15(op, args, stream, sms);
+    case 16: return gfpa_launch_cfg16(op, args, stream, sms);
+    case 17: return gfpa_launch_cfg17(op, args, stream, sms);
   }
   return cudaErrorInvalidValue;
 }

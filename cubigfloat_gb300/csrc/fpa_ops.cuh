@@ -14,8 +14,8 @@ namespace gfpa {
 template <int G, int K, int R>
 struct OpSpace {
   static constexpr int N = G * K * R;
-  __host__ __device__ static constexpr int addsub() { return 3 * N + 8; }
-  __host__ __device__ static constexpr int mul() { return 2 * N + 4; }
+  __host__ __device__ static constexpr int addsub() { return 5 * N + 8; }   // 2 staged pairs + X
+  __host__ __device__ static constexpr int mul() { return 2 * N + 4 + 2 * N + 2 * K; }   // P + 2nd staged pair
   __host__ __device__ static constexpr int div() { return (N + 4) * 2 + (2 * N + 8) * 2 + (N + 8); }
   __host__ __device__ static constexpr int sqrt() { return (N + 4) * 3 + (N + 8) * 4 + (2 * N + 8); }
   __host__ __device__ static constexpr int max_all() {
@@ -71,20 +71,15 @@ __device__ __forceinline__ uint32_t exp_word(long long e, uint32_t sign) {
 // (X, X+1) (d > 64 implies at most one bit of cancellation, so 63 guard bits remain).
 // Range: effective add -> +-INF when BIAS+e > 0x7FFFFFFF (:118-119); effective
 // subtraction -> +-TINY when BIAS+e < 5 (:226-227, :272-273).
-template <int G, int K, int R>
-__device__ void op_addsub(const Grp<G> &g, uint32_t *ws, int n, int mode, int is_sub,
-                          uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
-                          uint32_t *r_exp, uint32_t *r) {
-  constexpr int N = G * K * R;
+template <int G>
+__device__ void op_addsub_staged(const Grp<G> &g, uint32_t *X, int n, int mode, int is_sub,
+                                 uint32_t a_exp, const uint32_t *sA, uint32_t b_exp, const uint32_t *sB,
+                                 uint32_t *r_exp, uint32_t *r) {
   const uint32_t act = c_action[is_sub][classify(a_exp) * 9 + classify(b_exp)];
-  if (act == ACT_COPY_A) { copy_value<G>(g, r_exp, r, n, a_exp, a); return; }
-  if (act == ACT_COPY_B) { copy_value<G>(g, r_exp, r, n, b_exp, b); return; }
-  if (act == ACT_NEG_B) { copy_value<G>(g, r_exp, r, n, b_exp ^ 1u, b); return; }   // 0 - b = -b
+  if (act == ACT_COPY_A) { copy_value<G>(g, r_exp, r, n, a_exp, sA); return; }
+  if (act == ACT_COPY_B) { copy_value<G>(g, r_exp, r, n, b_exp, sB); return; }
+  if (act == ACT_NEG_B) { copy_value<G>(g, r_exp, r, n, b_exp ^ 1u, sB); return; }   // 0 - b = -b
   if (act != ACT_ADD && act != ACT_SUB) { write_class<G>(g, r_exp, act); return; }
-
-  uint32_t *sA = ws, *sB = sA + N, *X = sB + N;     // no product scratch needed
-  for (int i = g.lane; i < n; i += G) { sA[i] = a[i]; sB[i] = b[i]; }
-  g.sync();
   const uint32_t sa = a_exp & 1u, sb = (b_exp & 1u) ^ (uint32_t)is_sub;
   const long long ea = (long long)(a_exp >> 1) - BIAS, eb = (long long)(b_exp >> 1) - BIAS;
   const bool eff_sub = sa != sb;
@@ -120,9 +115,43 @@ __device__ void op_addsub(const Grp<G> &g, uint32_t *ws, int n, int mode, int is
   write_value<G>(g, r_exp, r, n, res, exp_word(e, sign));
 }
 
+// add/sub with operands anywhere: copies and class results straight from the operands,
+// otherwise the operands are staged in the workspace first (they are read several times).
+template <int G, int K, int R>
+__device__ void op_addsub(const Grp<G> &g, uint32_t *ws, int n, int mode, int is_sub,
+                          uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
+                          uint32_t *r_exp, uint32_t *r) {
+  constexpr int N = G * K * R;
+  const uint32_t act = c_action[is_sub][classify(a_exp) * 9 + classify(b_exp)];
+  if (act != ACT_ADD && act != ACT_SUB) {
+    op_addsub_staged<G>(g, ws, n, mode, is_sub, a_exp, a, b_exp, b, r_exp, r);
+    return;
+  }
+  uint32_t *sA = ws, *sB = sA + N, *X = sB + N;     // no product scratch needed
+  for (int i = g.lane; i < n; i += G) { sA[i] = a[i]; sB[i] = b[i]; }
+  g.sync();
+  op_addsub_staged<G>(g, X, n, mode, is_sub, a_exp, sA, b_exp, sB, r_exp, r);
+}
+
 // ---------------------------------------------------------------------------------------
 // mul.  Reference: fpa_warp_mul.h:41-139.  Exact 2n-limb product, one rounding.
 // Range (:124-128): TINY when BIAS+e < 5, INF when BIAS+e > 0x7FFFFFFF.
+template <int G, int K, int R>
+__device__ __forceinline__ void op_mul_staged(const Grp<G> &g, const MulScratch<G, K, R> &s, uint32_t *P, int n,
+                                              int mode, uint32_t a_exp, uint32_t b_exp, uint32_t *r_exp,
+                                              uint32_t *r) {
+  const uint32_t act = c_action[2][classify(a_exp) * 9 + classify(b_exp)];
+  if (act != ACT_MUL) { write_class<G>(g, r_exp, act); return; }
+  grp_mulsq_staged<G, K, R>(g, P, n, s);
+  const uint32_t sign = (a_exp ^ b_exp) & 1u;
+  Rounded res;
+  grp_round<G>(g, P, 2 * n, n, 0u, mode, sign, res);
+  const long long e = (long long)(a_exp >> 1) + (long long)(b_exp >> 1) - 2LL * BIAS - 64LL * n + res.L + res.ovf;
+  if ((long long)BIAS + e < 5) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
+  if ((long long)BIAS + e > 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
+  write_value<G>(g, r_exp, r, n, res, exp_word(e, sign));
+}
+
 template <int G, int K, int R>
 __device__ void op_mul(const Grp<G> &g, uint32_t *ws, int n, int mode,
                        uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
@@ -135,14 +164,7 @@ __device__ void op_mul(const Grp<G> &g, uint32_t *ws, int n, int mode,
   for (int i = g.lane; i < NK; i += G) s.sa[i] = (i < n) ? a[i] : 0u;
   for (int i = g.lane; i < NK + 2 * K; i += G) { int j = i - K; s.sb[i] = (j >= 0 && j < n) ? b[j] : 0u; }
   g.sync();
-  grp_mulsq_staged<G, K, R>(g, P, n, s);
-  const uint32_t sign = (a_exp ^ b_exp) & 1u;
-  Rounded res;
-  grp_round<G>(g, P, 2 * n, n, 0u, mode, sign, res);
-  const long long e = (long long)(a_exp >> 1) + (long long)(b_exp >> 1) - 2LL * BIAS - 64LL * n + res.L + res.ovf;
-  if ((long long)BIAS + e < 5) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
-  if ((long long)BIAS + e > 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
-  write_value<G>(g, r_exp, r, n, res, exp_word(e, sign));
+  op_mul_staged<G, K, R>(g, s, P, n, mode, a_exp, b_exp, r_exp, r);
 }
 
 // ---------------------------------------------------------------------------------------

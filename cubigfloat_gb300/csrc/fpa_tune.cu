@@ -61,7 +61,7 @@ extern "C" fpa_result fpa_gb300_autotune(fpa_op op, uint32_t limbs, uint32_t sam
   const uint32_t need = limbs < 4 ? 4 : limbs;
   for (int c = 0; c < GFPA_NUM_CFGS; c++) {
     const uint32_t cap = (uint32_t)gfpa_cfg_capacity(c);
-    if (cap < need || cap > 4 * (need < 8 ? 8 : need)) continue;
+    if (cap < need || cap > 4 * (need < 8 ? 8 : need) || !gfpa_cfg_supports(c, (int)op)) continue;
     ElementwiseArgs a;
     a.count = sample; a.n = limbs; a.mode = fpa_round_ties_to_even;
     a.r_exps = re; a.r_limbs = rl; a.a_exps = ae; a.a_limbs = al; a.b_exps = be; a.b_limbs = bl; a.err = err;
