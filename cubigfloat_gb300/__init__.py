@@ -73,6 +73,7 @@ def lib():
         "fpa_mul": (i32, [P, P, P, i32]),
         "fpa_div": (i32, [P, P, P, i32]),
         "fpa_sqrt": (i32, [P, P, i32]),
+        "fpa_gb300_fma": (i32, [P, P, P, P, i32]),
         "fpa_gb300_elementwise": (i32, [i32, u32, u64, i32, vp, vp, vp, vp, vp, vp, vp]),
         "fpa_op_async": (i32, [i32, P, P, P, i32, vp]),
         "fpa_copy_array_to_device_async": (i32, [P, vp, vp, vp]),
@@ -187,6 +188,11 @@ def fpa_div(r, a, b, mode):
 
 def fpa_sqrt(r, x, mode):
     return lib().fpa_sqrt(r.ref, x.ref, mode)
+
+
+def fpa_fma(r, a, b, c, mode):
+    """fpa_gb300_fma: r = RND(a*b + c) with one rounding."""
+    return lib().fpa_gb300_fma(r.ref, a.ref, b.ref, c.ref, mode)
 
 
 def fpa_neg(r, a):

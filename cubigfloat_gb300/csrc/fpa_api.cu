@@ -233,6 +233,30 @@ fpa_result fpa_gb300_elementwise(fpa_op op, uint32_t precision, uint64_t count, 
                             (cudaStream_t)stream);
 }
 
+// r = RND(a*b + c), one rounding (no counterpart in the reference); argument checks as
+// fpa_dispatch.h:175-183 (counts first, then precisions)
+fpa_result fpa_gb300_fma(fpa_t r, fpa_t a, fpa_t b, fpa_t c, fpa_rounding_mode mode) {
+  const uint32_t count = r->count, precision = r->precision;
+  if (count != a->count || count != b->count || count != c->count) return fpa_invalid_counts;
+  if (precision != a->precision || precision != b->precision || precision != c->precision)
+    return fpa_invalid_precisions;
+  if (!valid_precision(precision)) return fpa_invalid_precisions;
+  if ((int)mode < 0 || (int)mode > 4) return fpa_math_error;
+  if (count == 0) return fpa_success;
+  int sms; uint32_t *err;
+  if (!ctx(sms, err)) return fpa_device_error;
+  ElementwiseArgs args;
+  args.count = count; args.n = precision / 32; args.mode = (int)mode;
+  args.r_exps = r->gpu_exps; args.r_limbs = r->gpu_limbs;
+  args.a_exps = a->gpu_exps; args.a_limbs = a->gpu_limbs;
+  args.b_exps = b->gpu_exps; args.b_limbs = b->gpu_limbs;
+  args.c_exps = c->gpu_exps; args.c_limbs = c->gpu_limbs;
+  args.err = err;
+  const int cfg = gfpa_default_cfg(args.n < 4 ? 4 : args.n);
+  if (cfg < 0) return fpa_invalid_precisions;
+  return gfpa_launch(cfg, GFPA_OP_FMA, &args, 0, sms) == cudaSuccess ? fpa_success : fpa_device_error;
+}
+
 fpa_result fpa_op_async(fpa_op op, fpa_t r, fpa_t a, fpa_t b, fpa_rounding_mode mode, void *stream) {
   if ((int)op == 4) return unary_op(4, r, a, mode, (cudaStream_t)stream);
   if ((int)op < 0 || (int)op > 4) return fpa_math_error;

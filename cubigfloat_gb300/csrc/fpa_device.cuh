@@ -27,7 +27,7 @@ enum : uint32_t {
   ACT_MUL = 16, ACT_DIV = 17, ACT_SQRT = 18, ACT_ADD = 20, ACT_SUB = 21,
   ACT_COPY_A = 22, ACT_COPY_B = 23, ACT_NEG_B = 24
 };
-enum : int { OP_ADD = 0, OP_SUB = 1, OP_MUL = 2, OP_DIV = 3, OP_SQRT = 4 };
+enum : int { OP_ADD = 0, OP_SUB = 1, OP_MUL = 2, OP_DIV = 3, OP_SQRT = 4, OP_FMA = 5 };
 
 // Special-value tables, rows = class of a, columns = class of b.  Same entries as the
 // reference's tables (fpa_warp_add_sub.h:15-39, fpa_warp_mul.h:1-12, fpa_warp_div.h:1-12,

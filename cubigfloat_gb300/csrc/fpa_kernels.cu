@@ -86,7 +86,7 @@
 namespace gfpa {
 
 template <int OP, int G, int K, int R>
-using Words = OpWords<OP, G, K, R>;
+using Words = PipeWords<OP, G, K, R>;
 
 // Register budgets (blocks of 128 threads per SM): 64 registers per thread for add/sub/mul
 // with tiles up to 4 limbs, 128 for 8-limb tiles and for div/sqrt (whose Newton loops keep
@@ -97,7 +97,8 @@ using Words = OpWords<OP, G, K, R>;
 template <int OP, int K>
 struct MinBlocks {
   static constexpr int v = (K >= 16) ? 2
-                           : ((OP == OP_DIV || OP == OP_SQRT) ? (K >= 8 ? 4 : GFPA_NEWTON_MINBLOCKS) : (K >= 8 ? 4 : 8));
+                           : ((OP == OP_DIV || OP == OP_SQRT || OP == OP_FMA) ? (K >= 8 ? 4 : GFPA_NEWTON_MINBLOCKS)
+                                                                               : (K >= 8 ? 4 : 8));
 };
 
 // add/sub: HBM-bound, so each group double-buffers its operands: the copies of its next
@@ -211,8 +212,11 @@ __global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(Elemen
     else if (OP == OP_DIV)
       op_div<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
                    args.r_exps + i, args.r_limbs + off, args.err);
-    else
+    else if (OP == OP_SQRT)
       op_sqrt<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, args.r_exps + i, args.r_limbs + off, args.err);
+    else
+      op_fma<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off, args.c_exps[i],
+                      args.c_limbs + off, args.r_exps + i, args.r_limbs + off);
     g.sync();   // the group's shared slice is reused by its next instance
   }
 }
@@ -263,6 +267,9 @@ extern "C" cudaError_t GFPA_LAUNCH_NAME(int op, const ElementwiseArgs *args, cud
     case OP_MUL: return launch_op<OP_MUL>(*args, stream, sms);
     case OP_DIV: return launch_op<OP_DIV>(*args, stream, sms);
     case OP_SQRT: return launch_op<OP_SQRT>(*args, stream, sms);
+#if GFPA_CFG <= 6
+    case OP_FMA: return launch_op<OP_FMA>(*args, stream, sms);   // default configurations only
+#endif
   }
   return cudaErrorInvalidValue;
 }

@@ -5,7 +5,8 @@
 
 // One elementwise launch: `count` instances of `n` limbs each, contiguous per instance
 // (instance i's limbs at i*n), exponent words in separate arrays.  All pointers are device
-// pointers.  b_* are ignored for sqrt.  `err` is a device word the kernels OR error bits
+// pointers.  b_* are ignored for sqrt; c_* are read by fma only (op 5, which the default
+// configurations 0..6 run).  `err` is a device word the kernels OR error bits
 // into (1: div correction did not converge, 2: sqrt correction did not converge).
 struct ElementwiseArgs {
   uint64_t count;
@@ -15,9 +16,11 @@ struct ElementwiseArgs {
   const uint32_t *a_exps, *a_limbs;
   const uint32_t *b_exps, *b_limbs;
   uint32_t *err;
+  const uint32_t *c_exps = nullptr, *c_limbs = nullptr;   // third operand (fma only)
 };
 
 #define GFPA_NUM_CFGS 18
+#define GFPA_OP_FMA 5        // elementwise operation code of fma (after add, sub, mul, div, sqrt)
 #define GFPA_NUM_DEFAULT_CFGS 7
 #define GFPA_MAX_LIMBS 512
 

@@ -14,10 +14,11 @@ namespace gfpa {
 template <int G, int K, int R>
 struct OpSpace {
   static constexpr int N = G * K * R;
-  __host__ __device__ static constexpr int addsub() { return 5 * N + 8; }   // 2 staged pairs + X
-  __host__ __device__ static constexpr int mul() { return 2 * N + 4 + 2 * N + 2 * K; }   // P + 2nd staged pair
+  __host__ __device__ static constexpr int addsub() { return 3 * N + 8; }   // staged a, b + X
+  __host__ __device__ static constexpr int mul() { return 2 * N + 4; }
   __host__ __device__ static constexpr int div() { return (N + 4) * 2 + (2 * N + 8) * 2 + (N + 8); }
   __host__ __device__ static constexpr int sqrt() { return (N + 4) * 3 + (N + 8) * 4 + (2 * N + 8); }
+  __host__ __device__ static constexpr int fma() { return (2 * N + 4) + (3 * N + 8); }      // P + sum window
   __host__ __device__ static constexpr int max_all() {
     int a = addsub(), b = mul(), c = div(), d = sqrt();
     int m = a > b ? a : b; m = m > c ? m : c; m = m > d ? m : d;
@@ -32,7 +33,19 @@ struct OpWords {
   __host__ __device__ static constexpr int v() {
     return (OP == OP_ADD || OP == OP_SUB) ? OpSpace<G, K, R>::addsub()
            : MulScratch<G, K, R>::words() + (OP == OP_MUL ? OpSpace<G, K, R>::mul()
-                                          : OP == OP_DIV ? OpSpace<G, K, R>::div() : OpSpace<G, K, R>::sqrt());
+                                          : OP == OP_DIV ? OpSpace<G, K, R>::div()
+                                          : OP == OP_SQRT ? OpSpace<G, K, R>::sqrt() : OpSpace<G, K, R>::fma());
+  }
+  __host__ __device__ static constexpr int aligned() { return (v() + 3) & ~3; }
+};
+
+// The elementwise kernels double-buffer the operands of add/sub and mul (the next
+// operation's copies are in flight while the group computes): one more staged pair each.
+template <int OP, int G, int K, int R>
+struct PipeWords {
+  static constexpr int N = G * K * R;
+  __host__ __device__ static constexpr int v() {
+    return OpWords<OP, G, K, R>::v() + ((OP == OP_ADD || OP == OP_SUB) ? 2 * N : (OP == OP_MUL ? 2 * N + 2 * K : 0));
   }
   __host__ __device__ static constexpr int aligned() { return (v() + 3) & ~3; }
 };
@@ -165,6 +178,75 @@ __device__ void op_mul(const Grp<G> &g, uint32_t *ws, int n, int mode,
   for (int i = g.lane; i < NK + 2 * K; i += G) { int j = i - K; s.sb[i] = (j >= 0 && j < n) ? b[j] : 0u; }
   g.sync();
   op_mul_staged<G, K, R>(g, s, P, n, mode, a_exp, b_exp, r_exp, r);
+}
+
+// ---------------------------------------------------------------------------------------
+// fma: r = RND(a*b + c) with one rounding (no counterpart in the reference).  Special
+// values: the mul table gives the class of the exact product, the add table combines it
+// with c.  A product that is a value with c = 0 or tiny rounds like fpa_mul; otherwise the
+// exact 2n-limb product and c are summed exactly in a window of at most 3n+4 limbs (an
+// operand lying wholly more than 64 bits below the other's lowest bit matters only as a
+// sticky / borrow and is moved up to just below that guard) and rounded once.  Results
+// outside the exponent range become +-INF (BIAS+e > 0x7FFFFFFF) or +-TINY (BIAS+e < 5).
+template <int G>
+__device__ __forceinline__ int grp_bitlen(const Grp<G> &g, const uint32_t *X, int len) {
+  uint32_t top = 0;
+  for (int i = g.lane; i < len; i += G) if (X[i]) top = (uint32_t)i + 1u;
+  top = g.rmax(top);
+  return top == 0 ? 0 : 32 * ((int)top - 1) + 32 - (int)clz32(X[top - 1]);
+}
+
+template <int G, int K, int R>
+__device__ void op_fma(const Grp<G> &g, uint32_t *ws, int n, int mode, uint32_t a_exp, const uint32_t *a,
+                       uint32_t b_exp, const uint32_t *b, uint32_t c_exp, const uint32_t *c, uint32_t *r_exp,
+                       uint32_t *r) {
+  constexpr int N = G * K * R;
+  const uint32_t pm = c_action[2][classify(a_exp) * 9 + classify(b_exp)];
+  const uint32_t sp = (a_exp ^ b_exp) & 1u;
+  const uint32_t pcls = pm == ACT_MUL ? sp : pm;          // class of the exact product
+  const uint32_t act = c_action[0][pcls * 9 + classify(c_exp)];
+  if (act == ACT_COPY_B) { copy_value<G>(g, r_exp, r, n, c_exp, c); return; }
+  if (act != ACT_COPY_A && act != ACT_ADD && act != ACT_SUB) { write_class<G>(g, r_exp, act); return; }
+  MulScratch<G, K, R> s; s.carve(ws);
+  uint32_t *P = ws + MulScratch<G, K, R>::words(), *X = P + (2 * N + 4);
+  const int Mp = (n + K - 1) / K, NK = Mp * K;
+  for (int i = g.lane; i < NK; i += G) s.sa[i] = (i < n) ? a[i] : 0u;
+  for (int i = g.lane; i < NK + 2 * K; i += G) { int j = i - K; s.sb[i] = (j >= 0 && j < n) ? b[j] : 0u; }
+  g.sync();
+  grp_mulsq_staged<G, K, R>(g, P, n, s);
+  long long lowP = (long long)(a_exp >> 1) + (long long)(b_exp >> 1) - 2LL * BIAS - 64LL * n;   // a*b = P*2^lowP
+  if (act == ACT_COPY_A) {                                 // c is zero or tiny: the rounded product
+    Rounded res;
+    grp_round<G>(g, P, 2 * n, n, 0u, mode, sp, res);
+    const long long e = lowP + res.L + res.ovf;
+    if ((long long)BIAS + e < 5) { write_class<G>(g, r_exp, CLS_POS_TINY - sp); return; }
+    if ((long long)BIAS + e > 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sp); return; }
+    write_value<G>(g, r_exp, r, n, res, exp_word(e, sp));
+    return;
+  }
+  const uint32_t sc = c_exp & 1u;
+  const long long ec = (long long)(c_exp >> 1) - BIAS;
+  long long lowC = ec - 32LL * n, topC = ec;                // c = C*2^lowC, C normalized
+  long long topP = lowP + grp_bitlen<G>(g, P, 2 * n);
+  if (topC < lowP - 64) { lowC = lowP - 64 - 32LL * n; topC = lowC + 32LL * n; }
+  else if (topP < lowC - 64) { const long long sh = (lowC - 64 - 64LL * n) - lowP; lowP += sh; topP += sh; }
+  const long long lo = lowP < lowC ? lowP : lowC, hi = topP > topC ? topP : topC;
+  const int xl = (int)((hi - lo) >> 5) + 2;                // <= 3n + 4
+  const Shifted xp{P, 2 * n, (int)(lowP - lo)}, xc{c, n, (int)(lowC - lo)};
+  uint32_t sign = sp;
+  if (sp == sc) grp_add<G>(g, X, xp, xc, xl, 0u);
+  else {
+    const int cmp = grp_cmp<G>(g, xp, xc, xl);
+    if (cmp == 0) { write_class<G>(g, r_exp, CLS_ZERO); return; }   // exact cancellation
+    if (cmp > 0) grp_sub<G>(g, X, xp, xc, xl, 0u);
+    else { grp_sub<G>(g, X, xc, xp, xl, 0u); sign = sc; }
+  }
+  Rounded res;
+  grp_round<G>(g, X, xl, n, 0u, mode, sign, res);
+  const long long e = lo + res.L + res.ovf;
+  if ((long long)BIAS + e > 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
+  if ((long long)BIAS + e < 5) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
+  write_value<G>(g, r_exp, r, n, res, exp_word(e, sign));
 }
 
 // ---------------------------------------------------------------------------------------
@@ -317,8 +399,10 @@ __device__ __forceinline__ uint64_t isqrt64(uint64_t x) {
 //   A_ext = A * 2^(32n) (even e) or A * 2^(32n-1) (odd e), S* = sqrt(A_ext) in [2^(32n-1), 2^(32n)).
 //   1. Z ~ 2^(32k)/sqrt(x) by Newton on 1/sqrt: Z_k' = Z_k*2^(32(k'-k)) + Z_k*E/2^(96k+1),
 //      E = 2^(32(k'+2k)) - X_k' * Z_k^2   (X_k' = top k' limbs of A_ext).
-//   2. S = floor(A * Z / 2^(32n [+1])), one exact correction with R = A_ext - S^2 until
-//      0 <= R <= 2S.
+//   2. S from Z: for n >= 4 the last Newton level is replaced by one Karp-Markstein step
+//      (S0 = sqrt(x) to half precision from Z, S = S0 + Z (A_ext - S0^2) / 2), otherwise
+//      S = floor(A * Z / 2^(32n [+1])); then one exact correction with R = A_ext - S^2
+//      until 0 <= R <= 2S.
 //   3. X = 2S + [R > S], sticky = R != 0, rounded once (positive).
 template <int G, int K, int R>
 __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
@@ -348,7 +432,8 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   g.sync();
   int lv[24];
   const int nl = newton_levels(n, lv);
-  for (int li = 1; li < nl; li++) {
+  const bool km = n >= 4;                      // last level replaced by one Karp-Markstein step
+  for (int li = 1; li < (km ? nl - 1 : nl); li++) {
     const int k = lv[li - 1], kp = lv[li];
     // W = Z_k^2  (Z_k has k+1 limbs)
     grp_mulsq<G, K, R>(g, W, Ptr{Z, k + 1}, Ptr{Z, k + 1}, k + 1, s);
@@ -369,13 +454,37 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
     else grp_add<G>(g, Z2, zsh, M, kp + 1, 0u);
     uint32_t *tmp = Z; Z = Z2; Z2 = tmp;
   }
-  // S = floor(A * Z / 2^(32n + odd))   (n+1 limbs)
-  const uint32_t ztop = Z[n];
-  grp_mulsq<G, K, R>(g, V1, Ptr{a, n}, Ptr{Z, n}, n, s);
-  if (g.lane == 0) { V1[2 * n] = 0; V1[2 * n + 1] = 0; }
-  g.sync();
-  grp_add<G>(g, V1 + n, Ptr{V1 + n, n + 2}, SmallMul{a, n, ztop}, n + 2, 0u);
-  grp_copy<G>(g, S, Shifted{V1, 2 * n + 2, -(32 * n + odd)}, n + 1);
+  if (km) {
+    // Karp-Markstein: with Z = Z_h (h = the level below n, x = A_ext / 2^(64n)):
+    //   S0 = floor(Xt * Z / 2^(32(h+1))) ~ sqrt(x) 2^(32m), Xt = top m+1 limbs of A_ext,
+    //   D  = A_ext - S0^2 2^(64(n-m))   (kept from limb n-2 up: |D| < 2^(32(n-m+3)) there),
+    //   S  = S0 2^(32(n-m)) + floor(D Z / 2^(32(n+h)+1)),
+    // with m = n+1-h, so that both the error of Z and the quadratic term stay below one
+    // unit of S; the exact correction below removes what is left.
+    const int h = lv[nl - 2], m = n + 1 - h;
+    grp_mul<G, K, R>(g, V1, Ptr{Xh + (n - m), m + 1}, m + 1, Ptr{Z, h + 1}, h + 1, s);
+    uint32_t *S0 = Z2;                         // m+1 limbs
+    grp_copy<G>(g, S0, Ptr{V1 + (h + 1), m + 1}, m + 1);
+    grp_mulsq<G, K, R>(g, W, Ptr{S0, m + 1}, Ptr{S0, m + 1}, m + 1, s);
+    const int dl = n + 4;
+    const Shifted xs{Xh, n + 1, 32}, ss{W, 2 * m + 2, 32 * (n - 2 * m + 2)};
+    const bool dneg = grp_cmp<G>(g, xs, ss, dl) < 0;
+    if (dneg) grp_sub<G>(g, P, ss, xs, dl, 0u);
+    else grp_sub<G>(g, P, xs, ss, dl, 0u);
+    const int dlen = n - m + 3;
+    grp_mul<G, K, R>(g, V1, Ptr{P, dlen}, dlen, Ptr{Z, h + 1}, h + 1, s);
+    const Shifted s0s{S0, m + 1, 32 * (n - m)}, cs{V1, dlen + h + 1, -(32 * (h + 2) + 1)};
+    if (dneg) grp_sub<G>(g, S, s0s, cs, n + 1, 0u);
+    else grp_add<G>(g, S, s0s, cs, n + 1, 0u);
+  } else {
+    // S = floor(A * Z / 2^(32n + odd))   (n+1 limbs)
+    const uint32_t ztop = Z[n];
+    grp_mulsq<G, K, R>(g, V1, Ptr{a, n}, Ptr{Z, n}, n, s);
+    if (g.lane == 0) { V1[2 * n] = 0; V1[2 * n + 1] = 0; }
+    g.sync();
+    grp_add<G>(g, V1 + n, Ptr{V1 + n, n + 2}, SmallMul{a, n, ztop}, n + 2, 0u);
+    grp_copy<G>(g, S, Shifted{V1, 2 * n + 2, -(32 * n + odd)}, n + 1);
+  }
   // Rm = (A_ext - S^2) mod 2^(32(n+2)),  S = stop*2^(32n) + Slow
   const uint32_t stop = S[n];
   grp_mulsq<G, K, R>(g, V1, Ptr{S, n}, Ptr{S, n}, n, s);

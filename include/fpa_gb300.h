@@ -38,6 +38,12 @@ fpa_result fpa_copy_array_to_host_async(fpa_t fpa, uint32_t *exps, uint32_t *lim
  * device): 1 = a division's correction loop hit its bound, 2 = same for sqrt. */
 uint32_t fpa_gb300_device_errors(void);
 
+/* r = RND(a*b + c) with a single rounding (no counterpart in the reference, whose API has
+ * no fused operation).  All four arrays share count and precision; argument checks follow
+ * fpa_dispatch.h:175-183.  Special values: the class of the exact product from the mul
+ * table (fpa_warp_mul.h:1-12), combined with c by the add table (fpa_warp_add_sub.h:15-24). */
+fpa_result fpa_gb300_fma(fpa_t r, fpa_t a, fpa_t b, fpa_t c, fpa_rounding_mode mode);
+
 /* Lane-group configurations: configuration c runs one number per `lanes` threads with
  * product tiles of `tile_limbs` limbs, `pairs` column-block pairs per lane, and holds up
  * to lanes*tile_limbs*pairs limbs. */

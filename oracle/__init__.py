@@ -41,6 +41,8 @@ def lib():
         L.oracle_batch.argtypes = [i32, u32, i32, u32, vp, vp, vp, vp, vp, vp, i32]
         L.oracle_mixed.restype = i32
         L.oracle_mixed.argtypes = [u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32]
+        L.oracle_fma_batch.restype = i32
+        L.oracle_fma_batch.argtypes = [u32, i32, u32, vp, vp, vp, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -64,6 +66,18 @@ def run(op, n, mode, a_exps, a_limbs, b_exps=None, b_limbs=None, threads=1):
                             _p(b_exps) if op != SQRT else None, _p(b_limbs) if op != SQRT else None, threads)
     if rc != 0:
         raise ValueError(f"oracle_batch rc={rc}")
+    return r_exps, r_limbs
+
+
+def run_fma(n, mode, a_exps, a_limbs, b_exps, b_limbs, c_exps, c_limbs):
+    """r = RND(a*b + c) with one rounding over count instances; returns (r_exps, r_limbs)."""
+    arr = [np.ascontiguousarray(x, dtype=np.uint32) for x in (a_exps, a_limbs, b_exps, b_limbs, c_exps, c_limbs)]
+    count = arr[0].size
+    r_exps = np.zeros(count, dtype=np.uint32)
+    r_limbs = np.zeros((count, n), dtype=np.uint32)
+    rc = lib().oracle_fma_batch(n, mode, count, _p(r_exps), _p(r_limbs), *[_p(x) for x in arr])
+    if rc != 0:
+        raise ValueError(f"oracle_fma_batch rc={rc}")
     return r_exps, r_limbs
 
 

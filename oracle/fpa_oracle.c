@@ -433,6 +433,70 @@ static void op_sqrt(uint32_t n, int mode, uint32_t *r_exp, uint32_t *r_limbs,
   free(X); free(S); free(M);
 }
 
+/* Fused multiply-add r = RND(a*b + c) with one rounding.  The reference has no FMA; its
+ * special values follow the existing tables: the class of the exact product is the mul
+ * table's (fpa_warp_mul.h:1-12), then the add table (fpa_warp_add_sub.h:15-24) combines
+ * it with c.  A product that is a value and c = 0 / tiny rounds like fpa_mul; the sum of
+ * two values is exact before its single rounding, and a result outside the exponent range
+ * becomes +-INF (BIAS+e > 0x7FFFFFFF) or +-TINY (BIAS+e < 5). */
+static void op_fma(uint32_t n, int mode, uint32_t *r_exp, uint32_t *r_limbs,
+                   uint32_t a_exp, const uint32_t *a, uint32_t b_exp, const uint32_t *b,
+                   uint32_t c_exp, const uint32_t *c) {
+  uint32_t pm = mul_table[classify(a_exp) * 9 + classify(b_exp)];
+  int sp = (int)((a_exp ^ b_exp) & 1u);
+  uint32_t pcls = pm == A_MUL ? (uint32_t)sp : pm;       /* class of the exact product */
+  uint32_t action = add_table[pcls * 9 + classify(c_exp)];
+  if (action == A_COPY_B) { *r_exp = c_exp; memcpy(r_limbs, c, 4 * n); return; }
+  if (action != A_COPY_A && action != A_ADD && action != A_SUB) { *r_exp = action; return; }
+  int64_t ea = (int64_t)(a_exp >> 1) - BIAS, eb = (int64_t)(b_exp >> 1) - BIAS;
+  uint32_t *P = (uint32_t *)calloc(2 * n, 4), *M = (uint32_t *)malloc(4 * n);
+  mul_full(P, a, n, b, n);
+  int64_t lowP = ea + eb - 64LL * n;                     /* product = P * 2^lowP */
+  if (action == A_COPY_A) {                              /* c is zero or tiny: rounded product */
+    int64_t e = round_pack(n, mode, sp, P, 2 * n, lowP, 0, M);
+    if (BIAS + e < 5) *r_exp = C_POS_TINY - sp;
+    else if (BIAS + e > 0x7FFFFFFFLL) *r_exp = C_POS_INF - sp;
+    else { *r_exp = encode(e, sp); memcpy(r_limbs, M, 4 * n); }
+    free(P); free(M);
+    return;
+  }
+  int sc = (int)(c_exp & 1u);
+  int64_t ec = (int64_t)(c_exp >> 1) - BIAS, lowC = ec - 32LL * n;   /* c = C * 2^lowC */
+  int64_t topP = lowP + bitlen(P, 2 * n), topC = ec;
+  /* an operand entirely more than 64 bits below the other's lowest bit only matters as a
+   * sticky / borrow: move it up to just below that 64-bit guard (exact for rounding) */
+  if (topC < lowP - 64) { lowC = lowP - 64 - 32LL * n; topC = lowC + 32LL * n; }
+  else if (topP < lowC - 64) { int64_t sh = (lowC - 64 - 64LL * n) - lowP; lowP += sh; topP += sh; }
+  int64_t lo = lowP < lowC ? lowP : lowC, hi = topP > topC ? topP : topC;
+  int xl = (int)((hi - lo) >> 5) + 2;
+  uint32_t *X1 = (uint32_t *)calloc(xl, 4), *X2 = (uint32_t *)calloc(xl, 4);
+  shl_into(X1, xl, P, 2 * n, (int)(lowP - lo));
+  shl_into(X2, xl, c, n, (int)(lowC - lo));
+  int sign;
+  if (sp == sc) { add_into(X1, xl, X2, xl); sign = sp; }
+  else {
+    int cmp = cmp_n(X1, X2, xl);
+    if (cmp == 0) { *r_exp = C_ZERO; free(P); free(M); free(X1); free(X2); return; }
+    if (cmp > 0) { sub_into(X1, xl, X2, xl); sign = sp; }
+    else { sub_into(X2, xl, X1, xl); memcpy(X1, X2, 4 * (size_t)xl); sign = sc; }
+  }
+  int64_t e = round_pack(n, mode, sign, X1, xl, lo, 0, M);
+  if (BIAS + e > 0x7FFFFFFFLL) *r_exp = C_POS_INF - sign;
+  else if (BIAS + e < 5) *r_exp = C_POS_TINY - sign;
+  else { *r_exp = encode(e, sign); memcpy(r_limbs, M, 4 * n); }
+  free(P); free(M); free(X1); free(X2);
+}
+
+int oracle_fma_batch(uint32_t n, int mode, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs,
+                     const uint32_t *a_exps, const uint32_t *a_limbs, const uint32_t *b_exps,
+                     const uint32_t *b_limbs, const uint32_t *c_exps, const uint32_t *c_limbs) {
+  if (n == 0 || n > 4096 || mode < 0 || mode > 4) return -1;
+  for (uint32_t i = 0; i < count; i++)
+    op_fma(n, mode, r_exps + i, r_limbs + (size_t)i * n, a_exps[i], a_limbs + (size_t)i * n, b_exps[i],
+           b_limbs + (size_t)i * n, c_exps[i], c_limbs + (size_t)i * n);
+  return 0;
+}
+
 int oracle_op(int op, uint32_t n, int mode, uint32_t *r_exp, uint32_t *r_limbs,
               uint32_t a_exp, const uint32_t *a_limbs, uint32_t b_exp, const uint32_t *b_limbs) {
   if (n == 0 || n > 4096 || mode < 0 || mode > 4) return -1;

@@ -35,6 +35,13 @@ int oracle_op(int op, uint32_t n, int mode,
 
 /* Elementwise over `count` instances stored contiguously (exps[i], limbs[i*n..i*n+n)),
  * split over `threads` pthreads (threads<=1: run on the calling thread). */
+/* r = RND(a*b + c), one rounding, for `count` instances (no counterpart in the reference;
+ * special values: the mul table's class of the exact product combined with c by the add
+ * table).  Returns 0, or -1 for a bad mode/n. */
+int oracle_fma_batch(uint32_t n, int mode, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs,
+                     const uint32_t *a_exps, const uint32_t *a_limbs, const uint32_t *b_exps,
+                     const uint32_t *b_limbs, const uint32_t *c_exps, const uint32_t *c_limbs);
+
 int oracle_batch(int op, uint32_t n, int mode, uint32_t count,
                  uint32_t *r_exps, uint32_t *r_limbs,
                  const uint32_t *a_exps, const uint32_t *a_limbs,

@@ -36,6 +36,8 @@ def lib():
             vp, u32, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
             L.gold_batch.restype = i32
             L.gold_batch.argtypes = [i32, u32, i32, u32, vp, vp, vp, vp, vp, vp]
+            L.gold_batch3.restype = i32
+            L.gold_batch3.argtypes = [i32, u32, i32, u32, vp, vp, vp, vp, vp, vp, vp, vp]
             L.gold_version.restype = ctypes.c_char_p
             _lib = L
         except Exception as e:  # libmpfr absent
@@ -67,6 +69,18 @@ def run(op, n, mode, a_exps, a_limbs, b_exps=None, b_limbs=None):
     r_limbs = np.zeros((count, n), dtype=np.uint32)
     bad = lib().gold_batch(op, n, mode, count, _p(r_exps), _p(r_limbs), _p(a_exps), _p(a_limbs),
                            _p(b_exps) if op != 4 else None, _p(b_limbs) if op != 4 else None)
+    if bad:
+        raise ValueError(f"{bad} MPFR results were not finite")
+    return r_exps, r_limbs
+
+
+def run_fma(n, mode, a_exps, a_limbs, b_exps, b_limbs, c_exps, c_limbs):
+    """MPFR's correctly rounded a*b + c (mpfr_fma); inputs must be finite nonzero values."""
+    arr = [np.ascontiguousarray(x, dtype=np.uint32) for x in (a_exps, a_limbs, b_exps, b_limbs, c_exps, c_limbs)]
+    count = arr[0].size
+    r_exps = np.zeros(count, dtype=np.uint32)
+    r_limbs = np.zeros((count, n), dtype=np.uint32)
+    bad = lib().gold_batch3(5, n, mode, count, _p(r_exps), _p(r_limbs), *[_p(x) for x in arr])
     if bad:
         raise ValueError(f"{bad} MPFR results were not finite")
     return r_exps, r_limbs

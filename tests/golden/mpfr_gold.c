@@ -31,6 +31,7 @@ int mpfr_sub(mpfr_s *, const mpfr_s *, const mpfr_s *, int);
 int mpfr_mul(mpfr_s *, const mpfr_s *, const mpfr_s *, int);
 int mpfr_div(mpfr_s *, const mpfr_s *, const mpfr_s *, int);
 int mpfr_sqrt(mpfr_s *, const mpfr_s *, int);
+int mpfr_fma(mpfr_s *, const mpfr_s *, const mpfr_s *, const mpfr_s *, int);
 int mpfr_prec_round(mpfr_s *, mpfr_prec_t, int);
 int mpfr_zero_p(const mpfr_s *);
 int mpfr_nan_p(const mpfr_s *);
@@ -76,8 +77,9 @@ static int from_mpfr(uint32_t *exp, uint32_t *limbs, uint32_t n, const mpfr_s *x
   return words == n ? 0 : -2;
 }
 
-static int apply(int op, mpfr_s *r, const mpfr_s *a, const mpfr_s *b, int rnd) {
+static int apply(int op, mpfr_s *r, const mpfr_s *a, const mpfr_s *b, const mpfr_s *c, int rnd) {
   switch (op) {
+    case 5: return mpfr_fma(r, a, b, c, rnd);
     case 0: return mpfr_add(r, a, b, rnd);
     case 1: return mpfr_sub(r, a, b, rnd);
     case 2: return mpfr_mul(r, a, b, rnd);
@@ -87,24 +89,26 @@ static int apply(int op, mpfr_s *r, const mpfr_s *a, const mpfr_s *b, int rnd) {
   return 0;
 }
 
-/* op: 0 add, 1 sub, 2 mul, 3 div, 4 sqrt.  mode: fpa_rounding_mode (fpa.h:8-10);
- * ties-away is computed as a (p+1)-bit truncation followed by rounding away from
- * zero when the extra bit is set. Inputs must be finite nonzero values. */
-int gold_batch(int op, uint32_t n, int mode, uint32_t count,
-               uint32_t *r_exps, uint32_t *r_limbs,
-               const uint32_t *a_exps, const uint32_t *a_limbs,
-               const uint32_t *b_exps, const uint32_t *b_limbs) {
+/* op: 0 add, 1 sub, 2 mul, 3 div, 4 sqrt, 5 fma (a*b + c).  mode: fpa_rounding_mode
+ * (fpa.h:8-10); ties-away is computed as a (p+1)-bit truncation followed by rounding away
+ * from zero when the extra bit is set. Inputs must be finite nonzero values. */
+int gold_batch3(int op, uint32_t n, int mode, uint32_t count,
+                uint32_t *r_exps, uint32_t *r_limbs,
+                const uint32_t *a_exps, const uint32_t *a_limbs,
+                const uint32_t *b_exps, const uint32_t *b_limbs,
+                const uint32_t *c_exps, const uint32_t *c_limbs) {
   static const int map[4] = { RNDZ, RNDU, RNDD, RNDN };
-  mpfr_s a, b, r;
+  mpfr_s a, b, c, r;
   mpfr_prec_t p = 32L * n;
-  mpfr_init2(&a, p); mpfr_init2(&b, p); mpfr_init2(&r, p);
+  mpfr_init2(&a, p); mpfr_init2(&b, p); mpfr_init2(&c, p); mpfr_init2(&r, p);
   int bad = 0;
   for (uint32_t i = 0; i < count; i++) {
     to_mpfr(&a, a_exps[i], a_limbs + (size_t)i * n, n);
     if (op != 4) to_mpfr(&b, b_exps[i], b_limbs + (size_t)i * n, n);
+    if (op == 5) to_mpfr(&c, c_exps[i], c_limbs + (size_t)i * n, n);
     if (mode == 4) {
       mpfr_set_prec(&r, p + 1);
-      apply(op, &r, &a, &b, RNDZ);
+      apply(op, &r, &a, &b, &c, RNDZ);
       mpz_s z; __gmpz_init(&z);
       if (!mpfr_zero_p(&r) && !mpfr_nan_p(&r) && !mpfr_inf_p(&r)) {
         mpfr_get_z_2exp(&z, &r);
@@ -121,10 +125,17 @@ int gold_batch(int op, uint32_t n, int mode, uint32_t count,
       __gmpz_clear(&z);
     } else {
       mpfr_set_prec(&r, p);
-      apply(op, &r, &a, &b, map[mode]);
+      apply(op, &r, &a, &b, &c, map[mode]);
     }
     if (from_mpfr(r_exps + i, r_limbs + (size_t)i * n, n, &r) != 0) bad++;
   }
-  mpfr_clear(&a); mpfr_clear(&b); mpfr_clear(&r);
+  mpfr_clear(&a); mpfr_clear(&b); mpfr_clear(&c); mpfr_clear(&r);
   return bad;
+}
+
+int gold_batch(int op, uint32_t n, int mode, uint32_t count,
+               uint32_t *r_exps, uint32_t *r_limbs,
+               const uint32_t *a_exps, const uint32_t *a_limbs,
+               const uint32_t *b_exps, const uint32_t *b_limbs) {
+  return gold_batch3(op, n, mode, count, r_exps, r_limbs, a_exps, a_limbs, b_exps, b_limbs, NULL, NULL);
 }
