@@ -299,7 +299,9 @@ struct ResidualMag {
 // div.  Reference: fpa_warp_div.h:127-201.
 //   1. Y ~ 2^(64n)/B by Newton: Y_k' = Y_k*2^(32(k'-k)) + Y_k*E/2^(64k),
 //      E = 2^(32(k+k')) - B_k' * Y_k   (B_k' = top k' limbs of B).
-//   2. Q = floor(A*Y / 2^(32n)), then one exact correction: R = A*2^(32n) - Q*B is formed
+//   2. Q from Y: for n >= 4 the last Newton level is replaced by one Karp-Markstein step
+//      (q0 = A*Y_h to half precision, Q = q0 + Y_h * (A - q0*B)), otherwise
+//      Q = floor(A*Y / 2^(32n)); then one exact correction: R = A*2^(32n) - Q*B is formed
 //      from the low n+2 limbs and Q is stepped until 0 <= R < B.
 //   3. X = 2Q + [2R >= B], sticky = R != 0 (2R == B is impossible for a quotient of two
 //      precision-p numbers), rounded once.
@@ -325,7 +327,8 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   g.sync();
   int lv[24];
   const int nl = newton_levels(n, lv);
-  for (int li = 1; li < nl; li++) {
+  const bool km = n >= 4;                      // last level replaced by one Karp-Markstein step
+  for (int li = 1; li < (km ? nl - 1 : nl); li++) {
     const int k = lv[li - 1], kp = lv[li];
     const uint32_t *Bk = b + (n - kp);
     // T = B_k' * Y_k   (k' x (k+1) limbs)
@@ -341,13 +344,36 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
     else grp_add<G>(g, Y2, ysh, M, kp + 1, 0u);
     uint32_t *tmp = Y; Y = Y2; Y2 = tmp;
   }
-  // Q = floor(A * Y / 2^(32n)),  n+1 limbs;  Y = ytop*2^(32n) + Ylow
-  const uint32_t ytop = Y[n];
-  grp_mulsq<G, K, R>(g, T, Ptr{a, n}, Ptr{Y, n}, n, s);
-  if (g.lane == 0) { T[2 * n] = 0; T[2 * n + 1] = 0; }
-  g.sync();
-  grp_add<G>(g, T + n, Ptr{T + n, n + 2}, SmallMul{a, n, ytop}, n + 2, 0u);
-  grp_copy<G>(g, Q, Ptr{T + n, n + 2}, n + 1);
+  if (km) {
+    // Karp-Markstein: with Y = Y_h (h = the level below n, a = A/2^(32n), y = 2^(32n)/B):
+    //   q0 = floor(At * Y / 2^(32(h+1))) ~ a y 2^(32m), At = top m+1 limbs of A,
+    //   D  = (A 2^(32n) - q0 B 2^(32(n-m))) / 2^(32(n-2))   (|D| < 2^(32(n-m+3))),
+    //   Q  = q0 2^(32(n-m)) + floor(D Y / 2^(32(h+2))),
+    // with m = n+1-h as for sqrt; the exact correction below removes what is left.
+    const int h = lv[nl - 2], m = n + 1 - h;
+    grp_mul<G, K, R>(g, T, Ptr{a + (n - m - 1), m + 1}, m + 1, Ptr{Y, h + 1}, h + 1, s);
+    uint32_t *q0 = Y2;                         // m+1 limbs
+    grp_copy<G>(g, q0, Ptr{T + (h + 1), m + 1}, m + 1);
+    grp_mul<G, K, R>(g, P2, Ptr{q0, m + 1}, m + 1, Ptr{b, n}, n, s);
+    const int dl = n + 3;
+    const Shifted xa{a, n, 64}, xq{P2, n + m + 1, -32 * (m - 2)};
+    const bool dneg = grp_cmp<G>(g, xa, xq, dl) < 0;
+    if (dneg) grp_sub<G>(g, T, xq, xa, dl, 0u);
+    else grp_sub<G>(g, T, xa, xq, dl, 0u);
+    const int dlen = n - m + 3;
+    grp_mul<G, K, R>(g, P2, Ptr{T, dlen}, dlen, Ptr{Y, h + 1}, h + 1, s);
+    const Shifted qs{q0, m + 1, 32 * (n - m)}, cs{P2, dlen + h + 1, -32 * (h + 2)};
+    if (dneg) grp_sub<G>(g, Q, qs, cs, n + 1, 0u);
+    else grp_add<G>(g, Q, qs, cs, n + 1, 0u);
+  } else {
+    // Q = floor(A * Y / 2^(32n)),  n+1 limbs;  Y = ytop*2^(32n) + Ylow
+    const uint32_t ytop = Y[n];
+    grp_mulsq<G, K, R>(g, T, Ptr{a, n}, Ptr{Y, n}, n, s);
+    if (g.lane == 0) { T[2 * n] = 0; T[2 * n + 1] = 0; }
+    g.sync();
+    grp_add<G>(g, T + n, Ptr{T + n, n + 2}, SmallMul{a, n, ytop}, n + 2, 0u);
+    grp_copy<G>(g, Q, Ptr{T + n, n + 2}, n + 1);
+  }
   // Rm = (A * 2^(32n) - Q * B) mod 2^(32(n+2))
   const uint32_t qtop = Q[n];
   grp_mulsq<G, K, R>(g, P2, Ptr{Q, n}, Ptr{b, n}, n, s);
