@@ -102,7 +102,7 @@ def make_inputs(count, seed=20240):
     from cubigfloat_gb300 import workloads as W
     data = {}
     for i, op in enumerate(OPS):
-        data[op] = W.config2(op, seed + i, count=count, n=N_LIMBS)
+        data[op] = W.workload_4096(op, seed + i, count=count, n=N_LIMBS)
     return data
 
 
@@ -182,7 +182,7 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": "ops/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": "4096-bit mul/div/sqrt (config 2)", "limbs": N_LIMBS, "sample_ops":
+            "config": {"workload": "4096-bit mul/div/sqrt, 2^20 operands each", "limbs": N_LIMBS, "sample_ops":
                        sum(min(CPU_SAMPLE[o], count) for o in OPS), "mode": "ties_to_even"},
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -221,7 +221,7 @@ def extra_add_mul_1024(fpa, torch, count=1 << 22):
     HBM-bound, so its roofline is bytes moved per second against the copy bandwidth."""
     from cubigfloat_gb300 import workloads as W
     n = 32
-    (ae, al), (be, bl) = W.config1(11, count=count, n=n)
+    (ae, al), (be, bl) = W.workload_1024(11, count=count, n=n)
     A, B, R = fpa.FpaArray(count, 32 * n), fpa.FpaArray(count, 32 * n), fpa.FpaArray(count, 32 * n)
     A.to_device(ae, al)
     B.to_device(be, bl)
@@ -534,7 +534,7 @@ def run_gb300(args):
     line = {"metric": METRIC, "value": value, "unit": "ops/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": "4096-bit mul/div/sqrt (config 2)", "limbs": n, "operands_per_op": count,
+            "config": {"workload": "4096-bit mul/div/sqrt, 2^20 operands each", "limbs": n, "operands_per_op": count,
                        "near_halfway_frac": 0.05, "mode": "ties_to_even", "step": "fpa_mul+fpa_div+fpa_sqrt",
                        "l2": "inputs 541 MB per operand array, larger than L2; no flush",
                        "parallelism": f"replicas x{world}"},

@@ -58,7 +58,7 @@ def reference_style(rng, count, n, shift_frac=5 / 8):
     return exps, limbs
 
 
-# ---- near-halfway constructions (config 2's 5% hard cases) ---------------------------
+# ---- near-halfway constructions (the 4096-bit workload's 5% hard cases) ---------------
 
 def _rand_bits(rng, bits):
     """random integer with exactly `bits` significant bits"""
@@ -123,7 +123,7 @@ def sqrt_near_exact(rng, n):
     return A, sq.bit_length() & 1
 
 
-def config2(op, seed, count=1 << 20, n=128, hard_frac=0.05, pool=256):
+def workload_4096(op, seed, count=1 << 20, n=128, hard_frac=0.05, pool=256):
     """4096-bit mul/div/sqrt operands: uniform mantissas, e in [-1000, 1000]; nonzero
     divisors, positive sqrt arguments; `hard_frac` of the instances are near-halfway
     (mul) or near-exact (div, sqrt) cases drawn from a pool of distinct constructions
@@ -149,7 +149,7 @@ def config2(op, seed, count=1 << 20, n=128, hard_frac=0.05, pool=256):
     return (a_exps, a_limbs), (b_exps, b_limbs)
 
 
-def config1(seed, count=65536, n=32):
+def workload_1024(seed, count=65536, n=32):
     """1024-bit add/mul operands: uniform mantissas, e in [-64, 64], random signs."""
     rng = np.random.default_rng(seed)
     a = uniform(rng, count, n, -64, 64)
@@ -162,8 +162,8 @@ MIX_P = np.array([0.3, 0.2, 0.3, 0.1, 0.1])
 
 
 def mixed(seed, count, min_bits=256, max_bits=16384, mode=3, hard_frac=0.05, ops=None, limbs=None):
-    """Mixed batch (config 3): op drawn 30/20/30/10/10 from add/sub/mul/div/sqrt, precision
-    log-uniform in [min_bits, max_bits] rounded to whole limbs, operands as in config 2
+    """Mixed batch (10^6-op workload): op drawn 30/20/30/10/10 from add/sub/mul/div/sqrt, precision
+    log-uniform in [min_bits, max_bits] rounded to whole limbs, operands as in the 4096-bit workload
     (uniform mantissas, e in [-1000, 1000], positive sqrt arguments, `hard_frac`
     near-halfway/near-exact cases, one construction per (op, limbs) pair).
     Returns (descs, a_exps, a_limbs_flat, b_exps, b_limbs_flat, r_total) with descs in the
@@ -226,8 +226,8 @@ SERVED_PRECISIONS = (512, 1024, 4096, 16384)
 
 
 def served_job(rng, precision=None, size=None, max_ops=4096):
-    """One served request (config 5): a precision from {512, 1024, 4096, 16384} bits, a size
-    log-uniform in [1, max_ops], ops drawn 30/20/30/10/10, operands as in config 2 without
+    """One served request: a precision from {512, 1024, 4096, 16384} bits, a size
+    log-uniform in [1, max_ops], ops drawn 30/20/30/10/10, operands as in the 4096-bit workload without
     the hard cases.  Returns (precision, ops, modes, a_exps, a_limbs, b_exps, b_limbs)."""
     if precision is None:
         precision = int(rng.choice(SERVED_PRECISIONS))

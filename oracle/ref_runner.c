@@ -1,5 +1,5 @@
 /*
- * ref_runner.c -- runs the reference's own GPU kernels (TEST / BASELINE INFRASTRUCTURE).
+ * ref_runner.c -- runs the reference's own GPU kernels (TEST INFRASTRUCTURE).
  *
  * Loads oracle/_ref/ref_fpa.cubin (the reference's fpa.cu compiled for sm_103a by
  * oracle.build_ref()) through the CUDA driver API and launches its kernels exactly as its

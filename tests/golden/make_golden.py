@@ -4,7 +4,7 @@ Run from the repository root:  python tests/golden/make_golden.py
 Writes tests/golden/fixtures/<op>_n<limbs>.npz with the operands (a_*, b_*) and, for each
 rounding mode m = 0..4, the MPFR result (r_exps[m], r_limbs[m]).  Operand sets per file:
 uniform mantissas, the reference test generator's limb pattern (tests.c:173-181) and the
-near-halfway / near-exact constructions of config 2.
+near-halfway / near-exact constructions of the 4096-bit workload.
 """
 import os
 import sys

@@ -1,4 +1,4 @@
-"""GPU: fused chains (config 4 shapes at small sizes) against the same operation sequence
+"""GPU: fused chains (the dot and Newton sqrt shapes at small sizes) against the same operation sequence
 run step by step in the oracle: dot products acc = RN(acc + RN(x*y)) and Newton square
 roots y = RN(RN(y + RN(x/y)) * 0.5)."""
 import numpy as np
