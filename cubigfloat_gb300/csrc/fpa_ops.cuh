@@ -16,8 +16,8 @@ struct OpSpace {
   static constexpr int N = G * K * R;
   __host__ __device__ static constexpr int addsub() { return 3 * N + 8; }   // staged a, b + X
   __host__ __device__ static constexpr int mul() { return 2 * N + 4; }
-  __host__ __device__ static constexpr int div() { return (N + 4) * 2 + (2 * N + 8) * 2 + (N + 8); }
-  __host__ __device__ static constexpr int sqrt() { return (N + 4) * 3 + (N + 8) * 4 + (2 * N + 8); }
+  __host__ __device__ static constexpr int div() { return (N / 2 + 8) * 2 + (N + 8) + (2 * N + 8) + (N + 8); }
+  __host__ __device__ static constexpr int sqrt() { return (N + 4) + (N / 2 + 8) * 3 + (N + 8) * 3 + (2 * N + 8); }
   __host__ __device__ static constexpr int fma() { return (2 * N + 4) + (3 * N + 8); }      // P + sum window
   __host__ __device__ static constexpr int max_all() {
     int a = addsub(), b = mul(), c = div(), d = sqrt();
@@ -454,10 +454,12 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   if (act != ACT_DIV) { write_class<G>(g, r_exp, act); return; }
   MulScratch<G, K, R> s; s.carve(ws);
   // the operands are read where they lie (a, b): only the quotient's state is staged
-  uint32_t *Y = ws + MulScratch<G, K, R>::words(), *Y2 = Y + (N + 4);
-  uint32_t *T = Y2 + (N + 4), *P2 = T + (2 * N + 8);
+  // With the Karp-Markstein last step Y never exceeds h+1 <= n/2+2 limbs and T never holds
+  // more than n+3 (n < 4 takes the full-level path, whose 2n+2-limb A*Y fits N+8 there).
+  uint32_t *Y = ws + MulScratch<G, K, R>::words(), *Y2 = Y + (N / 2 + 8);
+  uint32_t *T = Y2 + (N / 2 + 8), *P2 = T + (N + 8);
   uint32_t *Q = P2 + (2 * N + 8);
-  uint32_t *Rm = T;                  // T (A*Y) is dead once Q is copied out of it
+  uint32_t *Rm = T;                  // T is dead once Q is formed
   uint32_t *X = P2;                  // P2 (Q*B) is dead once Rm is formed
   if (g.lane == 0) {
     uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)b[n - 1];   // level 1: floor((2^64-1)/B_top)
@@ -578,12 +580,14 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   MulScratch<G, K, R> s; s.carve(ws);
   // A_ext = A * 2^(32n - odd) has 2n limbs of which the low n-1 are zero: only its top n+1
   // limbs Xh = A * 2^(32 - odd) are kept (A_ext limb i = Xh[i - (n-1)]).
+  // With the Karp-Markstein last step Z never exceeds h+1 <= n/2+2 limbs and the Newton
+  // products Z^2 and X*W[k'..] never 2k+2 <= n/2+5 (n < 4 takes the full-level path).
   uint32_t *Xh = ws + MulScratch<G, K, R>::words();
-  uint32_t *Z = Xh + (N + 4), *Z2 = Z + (N + 4);
-  uint32_t *W = Z2 + (N + 4);        // Z_k^2: 2k+2 <= n+4 limbs
-  uint32_t *V1 = W + (N + 8), *V2 = V1 + (2 * N + 8), *P = V2 + (N + 8), *S = P + (N + 8);
-  uint32_t *Rm = V2;                 // V2 (kp + 2k+2-kp <= n+4 limbs) is dead after the Newton loop
-  uint32_t *E = W;                   // W (Z^2) is dead after the Newton loop
+  uint32_t *Z = Xh + (N + 4), *Z2 = Z + (N / 2 + 8);
+  uint32_t *W = Z2 + (N / 2 + 8);    // Z_k^2, later S0^2 (2m+2 <= n+3) and the rounded integer
+  uint32_t *V1 = W + (N + 8), *V2 = V1 + (2 * N + 8), *P = V2 + (N / 2 + 8), *S = P + (N + 8);
+  uint32_t *Rm = P;                  // P (Z*E, then |D|) is dead once S is formed
+  uint32_t *E = W;                   // W is dead once S is formed
   const long long e = (long long)(a_exp >> 1) - BIAS;
   const int odd = (int)(e & 1);
   const long long h = (e + odd) / 2;           // exact: e + odd is even
