@@ -261,9 +261,10 @@ static cudaError_t launch_op(const ElementwiseArgs &args, cudaStream_t stream, i
   constexpr size_t warp_bytes = (size_t)(32 / G) * Words<OP, G, K, R>::aligned() * sizeof(uint32_t);
   constexpr size_t cta_max = 227 * 1024;
   if constexpr (warp_bytes > cta_max) return cudaErrorInvalidConfiguration;
-  // CTA of 4, 2 or 1 warps, whichever keeps the most warps resident on an SM: shared memory
-  // is granted per CTA, so where four warps' worth does not fit once more, a smaller CTA
-  // may still fit.
+  // CTA of 4, 2 or 1 warps: a smaller CTA is taken only when it keeps at least a quarter
+  // more warps resident on an SM (shared memory is granted per CTA, so where four warps'
+  // worth does not fit once more, a smaller CTA may still fit; measured, small CTAs are
+  // otherwise slightly slower).
   static int configured = 0, warps = 1, per_sm = 1;
   auto kern = k_elementwise<OP, G, K, R>;
   if (!configured) {
@@ -276,7 +277,7 @@ static cudaError_t launch_op(const ElementwiseArgs &args, cudaStream_t stream, i
       int blocks = 0;
       e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, 32 * w, w * warp_bytes);
       if (e != cudaSuccess) return e;
-      if (blocks * w > best) { best = blocks * w; warps = w; per_sm = blocks; }
+      if (4 * blocks * w >= 5 * best && blocks * w > best) { best = blocks * w; warps = w; per_sm = blocks; }
     }
     if (per_sm < 1) per_sm = 1;
     configured = 1;
