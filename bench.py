@@ -331,7 +331,7 @@ def extra_chains(fpa, torch, dots=10000, length=1024, newtons=10000):
                             "ms": ms_newton, "iterations_s": newtons * 8 / (ms_newton / 1e3)}}
 
 
-def extra_served(fpa, njobs=400, rates=(1000.0, 4000.0, None)):
+def extra_served(fpa, njobs=400, rates=(1000.0, 4000.0, 16000.0, None)):
     """Served request stream: jobs of 1..4096 ops at one precision from {512, 1024, 4096,
     16384} bits, Poisson arrivals at each rate (None = all jobs at once), through the
     continuous-batching request loop and through plain per-job launches."""

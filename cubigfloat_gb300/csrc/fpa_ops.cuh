@@ -17,7 +17,7 @@ struct OpSpace {
   __host__ __device__ static constexpr int addsub() { return 3 * N + 8; }   // staged a, b + X
   __host__ __device__ static constexpr int mul() { return 2 * N + 4; }
   __host__ __device__ static constexpr int div() { return (N / 2 + 8) * 2 + (N + 8) + (2 * N + 8) + (N + 8); }
-  __host__ __device__ static constexpr int sqrt() { return (N + 4) + (N / 2 + 8) * 3 + (N + 8) * 3 + (2 * N + 8); }
+  __host__ __device__ static constexpr int sqrt() { return (N + 4) + (N / 2 + 8) * 2 + (N + 8) * 3 + (2 * N + 8); }
   __host__ __device__ static constexpr int fma() { return (2 * N + 4) + (3 * N + 8); }      // P + sum window
   __host__ __device__ static constexpr int max_all() {
     int a = addsub(), b = mul(), c = div(), d = sqrt();
@@ -565,7 +565,8 @@ __device__ __forceinline__ uint64_t isqrt64(uint64_t x) {
 // sqrt.  Reference: fpa_warp_sqrt.h:195-254 (odd exponents are made even, :218-223).
 //   A_ext = A * 2^(32n) (even e) or A * 2^(32n-1) (odd e), S* = sqrt(A_ext) in [2^(32n-1), 2^(32n)).
 //   1. Z ~ 2^(32k)/sqrt(x) by Newton on 1/sqrt: Z_k' = Z_k*2^(32(k'-k)) + Z_k*E/2^(96k+1),
-//      E = 2^(32(k'+2k)) - X_k' * Z_k^2   (X_k' = top k' limbs of A_ext).
+//      E = 2^(32(k'+2k)) - (X_k' * Z_k) * Z_k   (X_k' = top k' limbs of A_ext; the low
+//      limbs of the inner product that cannot reach the limbs of E used are dropped).
 //   2. S from Z: for n >= 4 the last Newton level is replaced by one Karp-Markstein step
 //      (S0 = sqrt(x) to half precision from Z, S = S0 + Z (A_ext - S0^2) / 2), otherwise
 //      S = floor(A * Z / 2^(32n [+1])); then one exact correction with R = A_ext - S^2
@@ -581,11 +582,11 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   // A_ext = A * 2^(32n - odd) has 2n limbs of which the low n-1 are zero: only its top n+1
   // limbs Xh = A * 2^(32 - odd) are kept (A_ext limb i = Xh[i - (n-1)]).
   // With the Karp-Markstein last step Z never exceeds h+1 <= n/2+2 limbs and the Newton
-  // products Z^2 and X*W[k'..] never 2k+2 <= n/2+5 (n < 4 takes the full-level path).
+  // products stay below 3n/4+8 limbs (n < 4 takes the full-level path).
   uint32_t *Xh = ws + MulScratch<G, K, R>::words();
   uint32_t *Z = Xh + (N + 4), *Z2 = Z + (N / 2 + 8);
-  uint32_t *W = Z2 + (N / 2 + 8);    // Z_k^2, later S0^2 (2m+2 <= n+3) and the rounded integer
-  uint32_t *V1 = W + (N + 8), *V2 = V1 + (2 * N + 8), *P = V2 + (N / 2 + 8), *S = P + (N + 8);
+  uint32_t *W = Z2 + (N / 2 + 8);    // T2 (<= 3n/4+8 limbs), later S0^2 (2m+2 <= n+3) and the rounded integer
+  uint32_t *V1 = W + (N + 8), *P = V1 + (2 * N + 8), *S = P + (N + 8);
   uint32_t *Rm = P;                  // P (Z*E, then |D|) is dead once S is formed
   uint32_t *E = W;                   // W is dead once S is formed
   const long long e = (long long)(a_exp >> 1) - BIAS;
@@ -604,19 +605,16 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   const bool km = n >= 4;                      // last level replaced by one Karp-Markstein step
   for (int li = 1; li < (km ? nl - 1 : nl); li++) {
     const int k = lv[li - 1], kp = lv[li];
-    // W = Z_k^2  (Z_k has k+1 limbs)
-    grp_mulsq<G, K, R>(g, W, Ptr{Z, k + 1}, Ptr{Z, k + 1}, k + 1, s);
-    // V = X_k' * W = X*W[0..k') + (X*W[k'..2k+2)) << k'   (the second factor is short)
+    // V = X_k' Z_k^2 as (X_k' Z_k) Z_k: the low j = k-2 limbs of T1 = X_k' Z_k only reach V
+    // below limb 2k-1, the lowest limb of E that is read, so T2 = (T1 >> 32j) Z_k = V / 2^(32j)
     const uint32_t *Xk = Xh + (n + 1 - kp);             // top k' limbs of A_ext (k' <= n)
-    const int ls = 2 * k + 2 - kp;
-    grp_mulsq<G, K, R>(g, V1, Ptr{Xk, kp}, Ptr{W, kp}, kp, s);
-    grp_mul<G, K, R>(g, V2, Ptr{Xk, kp}, kp, Ptr{W + kp, ls}, ls, s);
-    const int L = kp + 2 * k, lenV = L + 1;
-    grp_add<G>(g, V1, Ptr{V1, 2 * kp}, Shifted{V2, kp + ls, 32 * kp}, lenV, 0u);
-    // M = (Z_k * (|E| >> 32(2k-1))) >> (32(k+1) + 1),  E = 2^(32L) - V
-    const int lt = kp - k + 3;
-    const uint32_t neg = V1[L] != 0u;
-    grp_mul<G, K, R>(g, P, Ptr{Z, k + 1}, k + 1, ResidualMag{V1, 2 * k - 1, L, lt, neg}, lt, s);
+    grp_mul<G, K, R>(g, V1, Ptr{Xk, kp}, kp, Ptr{Z, k + 1}, k + 1, s);
+    const int j = k > 2 ? k - 2 : 0, l1 = kp + k + 1 - j;
+    grp_mul<G, K, R>(g, W, Ptr{V1 + j, l1}, l1, Ptr{Z, k + 1}, k + 1, s);
+    // M = (Z_k * (|E| >> 32(2k-1))) >> (32(k+1) + 1),  E = 2^(32(k'+2k)) - V
+    const int L = kp + 2 * k - j, lt = kp - k + 3;    // L: limb of 2^(32(k'+2k)) in T2
+    const uint32_t neg = W[L] != 0u;
+    grp_mul<G, K, R>(g, P, Ptr{Z, k + 1}, k + 1, ResidualMag{W, 2 * k - 1 - j, L, lt, neg}, lt, s);
     Shifted zsh{Z, k + 1, 32 * (kp - k)};
     Shifted M{P, k + 1 + lt, -(32 * (k + 1) + 1)};
     if (neg) grp_sub<G>(g, Z2, zsh, M, kp + 1, 0u);
