@@ -67,12 +67,12 @@ extern "C" fpa_result fpa_gb300_autotune(fpa_op op, uint32_t limbs, uint32_t sam
     a.r_exps = re; a.r_limbs = rl; a.a_exps = ae; a.a_limbs = al; a.b_exps = be; a.b_limbs = bl; a.err = err;
     if (gfpa_launch(c, (int)op, &a, 0, sms) != cudaSuccess) continue;     // warm-up (and attribute set-up)
     cudaEventRecord(e0);
-    for (int rep = 0; rep < 2; rep++) gfpa_launch(c, (int)op, &a, 0, sms);
+    for (int rep = 0; rep < 4; rep++) gfpa_launch(c, (int)op, &a, 0, sms);
     cudaEventRecord(e1);
     if (cudaEventSynchronize(e1) != cudaSuccess) break;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    const double rate = ms > 0.f ? 2.0 * sample / (ms * 1e-3) : 0.0;
+    const double rate = ms > 0.f ? 4.0 * sample / (ms * 1e-3) : 0.0;
     if (rate > best_rate) { best_rate = rate; best = c; }
   }
   cudaEventDestroy(e0); cudaEventDestroy(e1);

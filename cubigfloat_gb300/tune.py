@@ -20,14 +20,14 @@ OP_NAMES = ["add", "sub", "mul", "div", "sqrt"]
 DEFAULT_OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned_configs.txt")
 
 
-def tune(sample=1 << 15, ops=range(5), grid=GRID, log=print):
+def tune(sample=1 << 17, ops=range(5), grid=GRID, log=print):
     L = fpa.lib()
     table = []
     for op in ops:
         prev = 0
         for n in grid:
             best, rate = ctypes.c_int(-1), ctypes.c_double(0)
-            s = sample if n <= 128 else max(2048, sample // (n // 64))
+            s = sample if n <= 64 else max(4096, sample * 64 // n)       # about the same limbs per point
             rc = L.fpa_gb300_autotune(op, n, s, ctypes.byref(best), ctypes.byref(rate))
             if rc != fpa.fpa_success:
                 raise fpa.FpaError(f"fpa_gb300_autotune({op}, {n}) -> {rc}")
@@ -48,7 +48,7 @@ def write(table, path=DEFAULT_OUT):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--sample", type=int, default=1 << 15)
+    ap.add_argument("--sample", type=int, default=1 << 17)
     ap.add_argument("--out", default=DEFAULT_OUT)
     a = ap.parse_args()
     write(tune(a.sample), a.out)
