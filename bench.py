@@ -477,25 +477,69 @@ def run_gb300(args):
             assert fns[op](R, A, B, mode) == 0
             assert lib.fpa_copy_array_to_host(R.ref, vp(pr[0].data_ptr()), vp(pr[1].data_ptr())) == 0
 
-    e2e_step()
-    torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    t0 = time.perf_counter()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    f1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = f0.elapsed_time(f1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    # The same through the stream-ordered calls of the C ABI: operand copies, the operation
+    # and the result copy of each operation on three streams (host-to-device, compute,
+    # device-to-host), so that one operation's copies overlap another's compute.
+    s_in, s_op, s_out = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+    done = {op: None for op in OPS}        # compute of the previous step (its inputs are free after)
+    drained = {op: None for op in OPS}     # result copy of the previous step (its output is free after)
+
+    def e2e_step_streams():
+        for op in OPS:
+            A, B, R = arrs[op]
+            pa, pr = pinned[op]
+            if done[op] is not None:
+                s_in.wait_event(done[op])
+            assert lib.fpa_copy_array_to_device_async(A.ref, vp(pa[0].data_ptr()), vp(pa[1].data_ptr()),
+                                                      vp(s_in.cuda_stream)) == 0
+            if op != "sqrt":
+                assert lib.fpa_copy_array_to_device_async(B.ref, vp(pa[2].data_ptr()), vp(pa[3].data_ptr()),
+                                                          vp(s_in.cuda_stream)) == 0
+            e_in = torch.cuda.Event()
+            e_in.record(s_in)
+            s_op.wait_event(e_in)
+            if drained[op] is not None:
+                s_op.wait_event(drained[op])
+            assert lib.fpa_op_async(OP_CODE[op], R.ref, A.ref, (A if op == "sqrt" else B).ref, mode,
+                                    vp(s_op.cuda_stream)) == 0
+            done[op] = torch.cuda.Event()
+            done[op].record(s_op)
+            s_out.wait_event(done[op])
+            assert lib.fpa_copy_array_to_host_async(R.ref, vp(pr[0].data_ptr()), vp(pr[1].data_ptr()),
+                                                    vp(s_out.cuda_stream)) == 0
+            drained[op] = torch.cuda.Event()
+            drained[op].record(s_out)
+
+    def timed_e2e(step_fn, start_stream, end_stream):
+        step_fn()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(start_stream)
+        if start_stream is not stream:
+            for st in (s_in, s_op, s_out):
+                st.wait_event(g0)
+        for _ in range(args.steps):
+            step_fn()
+        if end_stream is not stream:
+            for st in (s_in, s_op):
+                end_stream.wait_stream(st)
+        g1.record(end_stream)
+        torch.cuda.synchronize()
+        ms = g0.elapsed_time(g1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    e2e_sync_ms = timed_e2e(e2e_step, stream, stream)
+    e2e_ms = timed_e2e(e2e_step_streams, s_in, s_out)
     h2d = sum((2 if op != "sqrt" else 1) * count * (4 + 4 * n) for op in OPS)
     d2h = len(OPS) * count * (4 + 4 * n)
     e2e_val = world * ops_per_step * args.steps / (e2e_ms / 1e3)
+    e2e_sync_val = world * ops_per_step * args.steps / (e2e_sync_ms / 1e3)
 
     gpu_results = None
     if rank == 0 and not args.no_cpu:
@@ -540,7 +584,11 @@ def run_gb300(args):
                        "parallelism": f"replicas x{world}"},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
             "e2e": {"value": e2e_val, "unit": "ops/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "api": "fpa_copy_array_to_device + fpa_mul/div/sqrt + fpa_copy_array_to_host (pinned)"},
+                    "api": "fpa_copy_array_to_device_async + fpa_op_async + fpa_copy_array_to_host_async "
+                           "(pinned host buffers; copy-in, compute and copy-out on three streams)",
+                    "sync": {"value": e2e_sync_val, "unit": "ops/s",
+                             "api": "fpa_copy_array_to_device + fpa_mul/div/sqrt + fpa_copy_array_to_host "
+                                    "(the fpa.h calls, one after another)"}},
             "gpu_launches": len(OPS) * args.steps,
             "extras": extras}
     print(json.dumps(line))
