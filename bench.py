@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the 1024-bit, mixed-batch, chained and served measurements")
     ap.add_argument("--quick-extras", action="store_true", help="smaller extra workloads")
+    ap.add_argument("--extras", default=",".join(EXTRAS), help="comma-separated extra workloads to run")
     return ap.parse_args()
 
 
@@ -235,7 +236,7 @@ def extra_add_mul_1024(fpa, torch, count=1 << 22):
             rec.update({"hbm_gbs": gbs, "hbm_peak_gbs": peak, "hbm_frac": gbs / peak, "peak_source": src})
         out[name] = rec
     del A, B, R
-    return {"workload": "1024-bit add and mul, 2^22 pairs, ties-to-even", **out}
+    return {"workload": f"1024-bit add and mul, {count} pairs, ties-to-even", **out}
 
 
 def extra_batched(fpa, torch, count):
@@ -369,13 +370,18 @@ def extra_served(fpa, njobs=400, rates=(1000.0, 4000.0, 16000.0, None)):
     return out
 
 
-def run_extras(fpa, torch, quick):
+EXTRAS = ("add_mul_1024", "batched_mixed", "chains", "served")
+
+
+def run_extras(fpa, torch, quick, only=EXTRAS):
     out = {}
-    for name, fn in (("add_mul_1024", lambda: extra_add_mul_1024(fpa, torch)),
+    for name, fn in (("add_mul_1024", lambda: extra_add_mul_1024(fpa, torch, 1 << 20 if quick else 1 << 22)),
                      ("batched_mixed", lambda: extra_batched(fpa, torch, 100000 if quick else 1000000)),
                      ("chains", lambda: extra_chains(fpa, torch, dots=1000 if quick else 10000,
                                                      newtons=1000 if quick else 10000)),
                      ("served", lambda: extra_served(fpa, njobs=100 if quick else 400))):
+        if name not in only:
+            continue
         t0 = time.perf_counter()
         try:
             out[name] = fn()
@@ -568,7 +574,7 @@ def run_gb300(args):
                            for op in OPS}}
     extras = None
     if not args.no_extras and world == 1:
-        extras = run_extras(fpa, torch, args.quick_extras)
+        extras = run_extras(fpa, torch, args.quick_extras, args.extras.split(","))
     cpu = None
     if not args.no_cpu:
         cpu = cpu_leg(data, gpu_results, os.cpu_count() or 1)

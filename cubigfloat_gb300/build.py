@@ -40,7 +40,7 @@ def _units():
     units = []
     for c in range(NUM_CFGS):
         units.append(("fpa_kernels.cu", [f"-DGFPA_CFG={c}"], f"fpa_kernels_cfg{c}.o"))
-    units.append(("fpa_thread_kernels.cu", [], "fpa_thread_kernels.o"))
+    units.append(("fpa_addsub_narrow.cu", [], "fpa_addsub_narrow.o"))
     units.append(("fpa_misc.cu", [], "fpa_misc.o"))
     units.append(("fpa_api.cu", [], "fpa_api.o"))
     units.append(("fpa_probe.cu", [], "fpa_probe.o"))

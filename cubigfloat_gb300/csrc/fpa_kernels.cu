@@ -5,6 +5,7 @@
 // so the configurations build in parallel.  Each object exports gfpa_launch_cfg<i>() used by the host dispatcher.
 #include <cuda_runtime.h>
 #include "fpa_ops.cuh"
+#include "fpa_addsub_regs.cuh"
 #include "fpa_launch.h"
 
 #ifndef GFPA_CFG
@@ -184,37 +185,6 @@ __device__ __forceinline__ void mul_pipelined(const Grp<G> &g, uint32_t *ws, con
   cp_async_wait<0>();
 }
 
-// add/sub of numbers that fit one limb per lane (n <= G): registers and shuffles only.
-template <int OP, int G>
-__global__ void __launch_bounds__(128, 8) k_addsub_reg(ElementwiseArgs args) {
-  Grp<G> g;
-  const uint32_t gpc = blockDim.x / G, gi = threadIdx.x / G;
-  const int n = (int)args.n;
-  for (uint64_t i = (uint64_t)blockIdx.x * gpc + gi; i < args.count; i += (uint64_t)gridDim.x * gpc) {
-    const uint64_t off = i * (uint64_t)n;
-    op_addsub_reg<G>(g, n, args.mode, OP == OP_SUB, args.a_exps[i], args.a_limbs + off, args.b_exps[i],
-                     args.b_limbs + off, args.r_exps + i, args.r_limbs + off);
-  }
-}
-
-template <int OP, int G>
-static cudaError_t launch_addsub_reg(const ElementwiseArgs &args, cudaStream_t stream, int sms) {
-  static int per_sm = 0;
-  auto kern = k_addsub_reg<OP, G>;
-  if (per_sm == 0) {
-    int b = 0;
-    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, 128, 0);
-    if (e != cudaSuccess) return e;
-    per_sm = b < 1 ? 1 : b;
-  }
-  constexpr int gpc = 128 / G;
-  const uint64_t need = (args.count + gpc - 1) / gpc, cap = (uint64_t)sms * per_sm;
-  const unsigned grid = (unsigned)(need < cap ? need : cap);
-  if (grid == 0) return cudaSuccess;
-  kern<<<grid, 128, 0, stream>>>(args);
-  return cudaGetLastError();
-}
-
 template <int OP, int G, int K, int R>
 __global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(ElementwiseArgs args) {
   extern __shared__ __align__(16) uint32_t smem[];
@@ -256,7 +226,7 @@ template <int OP>
 static cudaError_t launch_op(const ElementwiseArgs &args, cudaStream_t stream, int sms) {
   constexpr int G = CFG_G, K = CFG_K, R = CFG_R;
   if constexpr (OP == OP_ADD || OP == OP_SUB) {
-    if ((int)args.n <= G) return launch_addsub_reg<OP, G>(args, stream, sms);
+    if ((int)args.n <= G * K) return launch_addsub_regk<OP, G, K>(args, stream, sms);
   }
   constexpr size_t warp_bytes = (size_t)(32 / G) * Words<OP, G, K, R>::aligned() * sizeof(uint32_t);
   constexpr size_t cta_max = 227 * 1024;

@@ -28,13 +28,15 @@ struct ElementwiseArgs {
 // G*K*R limbs).  0..6 are the defaults in increasing capacity; 7..15 put two to eight
 // operations in one warp (fewer lanes per operation, wider tiles or several block pairs
 // per lane), which the autotuner can choose (mostly for div/sqrt); 16 and 17 run add/sub
-// with one thread per operation (capacity 32 and 64 limbs; fpa_thread_kernels.cu).
-static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4, 1, 1};
-static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4, 32, 64};
+// only, on groups of four lanes holding 8 or 16 limbs each in registers
+// (fpa_addsub_narrow.cu).
+static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4, 4, 4};
+static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4, 8, 16};
 static const int gfpa_cfg_R[GFPA_NUM_CFGS] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 2, 4, 2, 8, 1, 1};
 static inline int gfpa_cfg_capacity(int c) { return gfpa_cfg_G[c] * gfpa_cfg_K[c] * gfpa_cfg_R[c]; }
-// operations a configuration runs (the one-thread configurations run add/sub only)
-static inline bool gfpa_cfg_supports(int c, int op) { return gfpa_cfg_G[c] > 1 || op <= 1; }
+// configurations 16 and 17 run add/sub only
+static inline bool gfpa_cfg_addsub_only(int c) { return c >= 16; }
+static inline bool gfpa_cfg_supports(int c, int op) { return !gfpa_cfg_addsub_only(c) || op <= 1; }
 
 extern "C" {
 cudaError_t gfpa_launch_cfg0(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);

@@ -1,6 +1,6 @@
 """Autotune the lane-group configuration table on the current GPU.
 
-    python -m cubigfloat_gb300.tune [--sample N] [--out PATH]
+    python -m cubigfloat_gb300.tune [--sample N] [--out PATH] [--ops 0,1]
 
 For every operation and every limb count on a grid from 1 to 512, fpa_gb300_autotune times
 each configuration that can hold the limb count and keeps the fastest; each grid winner
@@ -28,6 +28,8 @@ def tune(sample=1 << 17, ops=range(5), grid=GRID, log=print):
         for n in grid:
             best, rate = ctypes.c_int(-1), ctypes.c_double(0)
             s = sample if n <= 64 else max(4096, sample * 64 // n)       # about the same limbs per point
+            if op in (0, 1):       # add/sub are bound by HBM: operands and results well beyond L2
+                s = max(s, (1 << 28) // (12 * (n + 1)))
             rc = L.fpa_gb300_autotune(op, n, s, ctypes.byref(best), ctypes.byref(rate))
             if rc != fpa.fpa_success:
                 raise fpa.FpaError(f"fpa_gb300_autotune({op}, {n}) -> {rc}")
@@ -38,7 +40,22 @@ def tune(sample=1 << 17, ops=range(5), grid=GRID, log=print):
     return table
 
 
+def read(path=DEFAULT_OUT):
+    """The (op, first, last, cfg, rate) rows of a table file."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("#") or not line.strip():
+                continue
+            head, _, tail = line.partition("#")
+            op, lo, hi, cfg = (int(x) for x in head.split())
+            rate = float(tail.split()[-1]) * 1e6 if tail.strip() else 0.0
+            rows.append((op, lo, hi, cfg, rate))
+    return rows
+
+
 def write(table, path=DEFAULT_OUT):
+    table = sorted(table, key=lambda r: (r[0], r[1]))
     with open(path, "w") as f:
         f.write("# op first_limbs last_limbs cfg   (autotuned on GB300 by cubigfloat_gb300.tune; "
                 "rates in M ops/s at the last limb count)\n")
@@ -50,6 +67,12 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--sample", type=int, default=1 << 17)
     ap.add_argument("--out", default=DEFAULT_OUT)
+    ap.add_argument("--ops", default="0,1,2,3,4", help="operations to tune; the rows of the others are "
+                    "kept from the current table")
     a = ap.parse_args()
-    write(tune(a.sample), a.out)
+    ops = sorted({int(x) for x in a.ops.split(",")})
+    table = tune(a.sample, ops)
+    if len(ops) < 5 and os.path.exists(DEFAULT_OUT):
+        table += [r for r in read(DEFAULT_OUT) if r[0] not in ops]
+    write(table, a.out)
     print("wrote", a.out)
