@@ -439,9 +439,11 @@ struct ResidualMag {
 //   1. Y ~ 2^(64n)/B by Newton: Y_k' = Y_k*2^(32(k'-k)) + Y_k*E/2^(64k),
 //      E = 2^(32(k+k')) - B_k' * Y_k   (B_k' = top k' limbs of B).
 //   2. Q from Y: for n >= 4 the last Newton level is replaced by one Karp-Markstein step
-//      (q0 = A*Y_h to half precision, Q = q0 + Y_h * (A - q0*B)), otherwise
-//      Q = floor(A*Y / 2^(32n)); then one exact correction: R = A*2^(32n) - Q*B is formed
-//      from the low n+2 limbs and Q is stepped until 0 <= R < B.
+//      (q0 = A*Y_h to half precision, Q = q0 + Y_h * (A - q0*B)) that yields one limb more
+//      than the result; when those 32 extra bits are clear of a rounding boundary they
+//      decide the rounding directly.  Otherwise (and for n < 4, Q = floor(A*Y / 2^(32n)))
+//      one exact correction: R = A*2^(32n) - Q*B is formed from the low n+2 limbs and Q is
+//      stepped until 0 <= R < B.
 //   3. X = 2Q + [2R >= B], sticky = R != 0 (2R == B is impossible for a quotient of two
 //      precision-p numbers), rounded once.
 // Range (:189-193): TINY when BIAS+e < 10, INF when BIAS+e >= 0x7FFFFFFF.
@@ -486,26 +488,46 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
     uint32_t *tmp = Y; Y = Y2; Y2 = tmp;
   }
   if (km) {
-    // Karp-Markstein: with Y = Y_h (h = the level below n, a = A/2^(32n), y = 2^(32n)/B):
+    // Karp-Markstein with one limb more than the result needs: with Y = Y_h (h = the level
+    // below n, a = A/2^(32n), y = 2^(32n)/B) and m = n+2-h,
     //   q0 = floor(At * Y / 2^(32(h+1))) ~ a y 2^(32m), At = top m+1 limbs of A,
-    //   D  = (A 2^(32n) - q0 B 2^(32(n-m))) / 2^(32(n-2))   (|D| < 2^(32(n-m+3))),
-    //   Q  = q0 2^(32(n-m)) + floor(D Y / 2^(32(h+2))),
-    // with m = n+1-h as for sqrt; the exact correction below removes what is left.
-    const int h = lv[nl - 2], m = n + 1 - h;
+    //   D  = (A 2^(32(n+1)) - q0 B 2^(32(h-1))) / 2^(32(n-2))   (|D| < 2^(32(m+2))),
+    //   Q' = q0 2^(32(h-1)) + floor(D Y / 2^(32(h+2)))  ~ (A/B) 2^(32(n+1)),  n+2 limbs.
+    // m is chosen so that the error of Y_h and the quadratic term stay within a few units
+    // of Q' (at most 9 over every size 4..512 in an exact integer simulation of these
+    // steps).  When the bits of Q' below the result's last place lie at least 2^20 units
+    // away from 0 and from one half, they decide the rounding on their own (round bit =
+    // their top bit, sticky = 1); otherwise floor(Q'/2^32) takes the exact correction.
+    const int h = lv[nl - 2], m = n + 2 - h;
     grp_mul<G, K, R>(g, T, Ptr{a + (n - m - 1), m + 1}, m + 1, Ptr{Y, h + 1}, h + 1, s);
     uint32_t *q0 = Y2;                         // m+1 limbs
     grp_copy<G>(g, q0, Ptr{T + (h + 1), m + 1}, m + 1);
     grp_mul<G, K, R>(g, P2, Ptr{q0, m + 1}, m + 1, Ptr{b, n}, n, s);
-    const int dl = n + 3;
-    const Shifted xa{a, n, 64}, xq{P2, n + m + 1, -32 * (m - 2)};
+    const int dl = n + 4;
+    const Shifted xa{a, n, 96}, xq{P2, n + m + 1, -32 * (n - h - 1)};
     const bool dneg = grp_cmp<G>(g, xa, xq, dl) < 0;
     if (dneg) grp_sub<G>(g, T, xq, xa, dl, 0u);
     else grp_sub<G>(g, T, xa, xq, dl, 0u);
-    const int dlen = n - m + 3;
+    const int dlen = m + 2;                    // <= n/2 + 4: within the group's capacity
     grp_mul<G, K, R>(g, P2, Ptr{T, dlen}, dlen, Ptr{Y, h + 1}, h + 1, s);
-    const Shifted qs{q0, m + 1, 32 * (n - m)}, cs{P2, dlen + h + 1, -32 * (h + 2)};
-    if (dneg) grp_sub<G>(g, Q, qs, cs, n + 1, 0u);
-    else grp_add<G>(g, Q, qs, cs, n + 1, 0u);
+    const Shifted qs{q0, m + 1, 32 * (h - 1)}, cs{P2, dlen + h + 1, -32 * (h + 2)};
+    if (dneg) grp_sub<G>(g, Q, qs, cs, n + 2, 0u);
+    else grp_add<G>(g, Q, qs, cs, n + 2, 0u);
+    // Q' lies in (2^(32n+31), 2^(32n+33)): 32 bits below the last place when Q'[n+1] = 0,
+    // else 33 (their top bit in Q'[1]); u = those bits without their top bit
+    const uint32_t qtop = Q[n + 1], u = qtop ? Q[0] : (Q[0] & 0x7FFFFFFFu);
+    const uint32_t umax = qtop ? 0xFFFFFFFFu : 0x7FFFFFFFu;
+    if (u >= (1u << 20) && u <= umax - (1u << 20)) {
+      const uint32_t sign = (a_exp ^ b_exp) & 1u;
+      Rounded res;
+      grp_round<G>(g, Q, n + 2, n, 1u, mode, sign, res);
+      const long long e = (long long)(a_exp >> 1) - (long long)(b_exp >> 1) - 32LL * n - 32 + res.L + res.ovf;
+      if ((long long)BIAS + e < 10) { write_class<G>(g, r_exp, CLS_POS_TINY - sign); return; }
+      if ((long long)BIAS + e >= 0x7FFFFFFFLL) { write_class<G>(g, r_exp, CLS_POS_INF - sign); return; }
+      write_value<G>(g, r_exp, r, n, res, exp_word(e, sign));
+      return;
+    }
+    Q += 1;                                    // floor(Q'/2^32): n+1 limbs, within one unit
   } else {
     // Q = floor(A * Y / 2^(32n)),  n+1 limbs;  Y = ytop*2^(32n) + Ylow
     const uint32_t ytop = Y[n];
@@ -591,7 +613,7 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   uint32_t *E = W;                   // W is dead once S is formed
   const long long e = (long long)(a_exp >> 1) - BIAS;
   const int odd = (int)(e & 1);
-  const long long h = (e + odd) / 2;           // exact: e + odd is even
+  const long long eh = (e + odd) / 2;          // exact: e + odd is even
   grp_copy<G>(g, Xh, Shifted{a, n, 32 - odd}, n + 1);
   if (g.lane == 0) {
     uint64_t x1 = (uint64_t)Xh[n] << 32;                   // top limb of A_ext, in [2^30, 2^32)
@@ -622,27 +644,40 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
     uint32_t *tmp = Z; Z = Z2; Z2 = tmp;
   }
   if (km) {
-    // Karp-Markstein: with Z = Z_h (h = the level below n, x = A_ext / 2^(64n)):
+    // Karp-Markstein with one limb more than the result needs: with Z = Z_h (h = the level
+    // below n, x = A_ext / 2^(64n)) and m = n+2-h,
     //   S0 = floor(Xt * Z / 2^(32(h+1))) ~ sqrt(x) 2^(32m), Xt = top m+1 limbs of A_ext,
-    //   D  = A_ext - S0^2 2^(64(n-m))   (kept from limb n-2 up: |D| < 2^(32(n-m+3)) there),
-    //   S  = S0 2^(32(n-m)) + floor(D Z / 2^(32(n+h)+1)),
-    // with m = n+1-h, so that both the error of Z and the quadratic term stay below one
-    // unit of S; the exact correction below removes what is left.
-    const int h = lv[nl - 2], m = n + 1 - h;
+    //   D  = (A_ext 2^64 - S0^2 2^(64(h-1))) / 2^(32(n-2))   (|D| < 2^(32(m+3))),
+    //   S' = S0 2^(32(h-1)) + floor(D Z / 2^(32(h+3)+1))  ~ sqrt(A_ext) 2^32,  n+2 limbs.
+    // m is chosen so that Z_h's error and the quadratic term stay within a few units of S'
+    // (at most 3 over every size 4..512 in an exact integer simulation of these steps).
+    // When the 32 bits of S' below the result's last place lie at least 2^20 units away
+    // from 0 and from one half, they decide the rounding on their own (round bit = their
+    // top bit, sticky = 1); otherwise floor(S'/2^32) takes the exact correction.
+    const int h = lv[nl - 2], m = n + 2 - h;
     grp_mul<G, K, R>(g, V1, Ptr{Xh + (n - m), m + 1}, m + 1, Ptr{Z, h + 1}, h + 1, s);
     uint32_t *S0 = Z2;                         // m+1 limbs
     grp_copy<G>(g, S0, Ptr{V1 + (h + 1), m + 1}, m + 1);
     grp_mulsq<G, K, R>(g, W, Ptr{S0, m + 1}, Ptr{S0, m + 1}, m + 1, s);
-    const int dl = n + 4;
-    const Shifted xs{Xh, n + 1, 32}, ss{W, 2 * m + 2, 32 * (n - 2 * m + 2)};
+    const int dl = n + 6;
+    const Shifted xs{Xh, n + 1, 96}, ss{W, 2 * m + 2, 32 * (2 * h - n)};
     const bool dneg = grp_cmp<G>(g, xs, ss, dl) < 0;
     if (dneg) grp_sub<G>(g, P, ss, xs, dl, 0u);
     else grp_sub<G>(g, P, xs, ss, dl, 0u);
-    const int dlen = n - m + 3;
+    const int dlen = m + 3;                    // <= n/2 + 5: within the group's capacity
     grp_mul<G, K, R>(g, V1, Ptr{P, dlen}, dlen, Ptr{Z, h + 1}, h + 1, s);
-    const Shifted s0s{S0, m + 1, 32 * (n - m)}, cs{V1, dlen + h + 1, -(32 * (h + 2) + 1)};
-    if (dneg) grp_sub<G>(g, S, s0s, cs, n + 1, 0u);
-    else grp_add<G>(g, S, s0s, cs, n + 1, 0u);
+    const Shifted s0s{S0, m + 1, 32 * (h - 1)}, cs{V1, dlen + h + 1, -(32 * (h + 3) + 1)};
+    if (dneg) grp_sub<G>(g, S, s0s, cs, n + 2, 0u);
+    else grp_add<G>(g, S, s0s, cs, n + 2, 0u);
+    // S' lies in [2^(32n+31), 2^(32n+32)) up to its error: 32 bits below the last place
+    const uint32_t u = S[0] & 0x7FFFFFFFu;
+    if (S[n + 1] == 0u && u >= (1u << 20) && u <= 0x7FFFFFFFu - (1u << 20)) {
+      Rounded res;
+      grp_round<G>(g, S, n + 1, n, 1u, mode, 0u, res);
+      write_value<G>(g, r_exp, r, n, res, exp_word(eh - 32LL * n - 32 + res.L + res.ovf, 0u));
+      return;
+    }
+    S += 1;                                    // floor(S'/2^32): n+1 limbs, within one unit
   } else {
     // S = floor(A * Z / 2^(32n + odd))   (n+1 limbs)
     const uint32_t ztop = Z[n];
@@ -682,7 +717,7 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   grp_add<G>(g, E, ShlBits{S, n + 1, 1}, Zero{}, n + 2, rb);
   Rounded res;
   grp_round<G>(g, E, n + 2, n, sticky, mode, 0u, res);
-  const long long er = h - 32LL * n - 1 + res.L + res.ovf;
+  const long long er = eh - 32LL * n - 1 + res.L + res.ovf;
   write_value<G>(g, r_exp, r, n, res, exp_word(er, 0u));
 }
 
