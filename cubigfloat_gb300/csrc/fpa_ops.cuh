@@ -435,6 +435,115 @@ struct ResidualMag {
 };
 
 // ---------------------------------------------------------------------------------------
+// The small Newton levels (k' <= SMALL_LEVEL limbs) of div and sqrt, run by one lane in
+// registers.  Group products cost a roughly fixed latency (staging, block sums, syncs)
+// however small they are, which made each of these levels as slow as a 17-limb one; here
+// every (k, k') pair is its own instantiation with compile-time sizes.  The steps and
+// truncations are exactly those of the group levels in op_div / op_sqrt, so the iterates
+// are the same integers.  Levels: k' = 2 comes from k = 1, otherwise k = floor((k'+2)/2).
+constexpr int SMALL_LEVEL = 9;
+
+// t = a * b (one thread)
+template <int LA, int LB>
+__device__ __forceinline__ void mul_regs(const uint32_t (&a)[LA], const uint32_t (&b)[LB], uint32_t (&t)[LA + LB]) {
+#pragma unroll
+  for (int i = 0; i < LA + LB; i++) t[i] = 0u;
+#pragma unroll
+  for (int i = 0; i < LA; i++) {
+    uint32_t carry = 0;
+#pragma unroll
+    for (int j = 0; j < LB; j++) {
+      const uint64_t x = (uint64_t)a[i] * b[j] + t[i + j] + carry;
+      t[i + j] = (uint32_t)x; carry = (uint32_t)(x >> 32);
+    }
+    t[i + LB] = carry;
+  }
+}
+
+// y' = y * 2^(32(kp-k)) +- (m >> sh) over kp+1 limbs (sh in {0, 1} bits; m of LM limbs,
+// read from limb MO up)
+template <int k, int kp, int LM, int MO>
+__device__ __forceinline__ void level_update(const uint32_t (&y)[k + 1], const uint32_t (&m)[LM], int sh, bool neg,
+                                             uint32_t (&out)[SMALL_LEVEL + 1]) {
+  uint32_t c = 0;
+#pragma unroll
+  for (int i = 0; i <= SMALL_LEVEL; i++) {
+    if (i > kp) { out[i] = 0u; continue; }
+    const uint32_t ys = (i >= kp - k) ? y[i - (kp - k)] : 0u;
+    const uint32_t lo = (MO + i < LM) ? m[MO + i] : 0u, hi = (MO + i + 1 < LM) ? m[MO + i + 1] : 0u;
+    const uint32_t mv = sh ? ((lo >> 1) | (hi << 31)) : lo;
+    if (!neg) { const uint64_t v = (uint64_t)ys + mv + c; out[i] = (uint32_t)v; c = (uint32_t)(v >> 32); }
+    else { const uint64_t v = (uint64_t)ys - mv - c; out[i] = (uint32_t)v; c = (uint32_t)(v >> 63); }
+  }
+}
+
+// div level k -> kp: T = B_kp * Y, E from T, Y' = Y 2^(32(kp-k)) +- (Y |E|) >> 32(k+1)
+template <int k, int kp>
+__device__ __forceinline__ void div_level_regs(const uint32_t (&bt)[SMALL_LEVEL], uint32_t (&y)[SMALL_LEVEL + 1]) {
+  constexpr int L = k + kp, lt = kp - k + 3;
+  uint32_t bk[kp], yk[k + 1], t[kp + k + 1], em[lt], p[k + 1 + lt];
+#pragma unroll
+  for (int i = 0; i < kp; i++) bk[i] = bt[SMALL_LEVEL - kp + i];
+#pragma unroll
+  for (int i = 0; i <= k; i++) yk[i] = y[i];
+  mul_regs<kp, k + 1>(bk, yk, t);
+  const bool neg = t[L] != 0u;
+#pragma unroll
+  for (int i = 0; i < lt; i++) em[i] = (k - 1 + i < L) ? (neg ? t[k - 1 + i] : ~t[k - 1 + i]) : 0u;
+  mul_regs<k + 1, lt>(yk, em, p);
+  level_update<k, kp, k + 1 + lt, k + 1>(yk, p, 0, neg, y);
+}
+
+// sqrt level k -> kp: V = (X_kp Z) Z without the low j = k-2 limbs of X_kp Z,
+// E = 2^(32(kp+2k)) - V, Z' = Z 2^(32(kp-k)) +- (Z |E|) >> (32(k+1)+1)
+template <int k, int kp>
+__device__ __forceinline__ void sqrt_level_regs(const uint32_t (&xt)[SMALL_LEVEL], uint32_t (&z)[SMALL_LEVEL + 1]) {
+  constexpr int j = k > 2 ? k - 2 : 0, l1 = kp + k + 1 - j, L = kp + 2 * k - j, lt = kp - k + 3;
+  uint32_t xk[kp], zk[k + 1], v1[kp + k + 1], t1[l1], w[l1 + k + 1], em[lt], p[k + 1 + lt];
+#pragma unroll
+  for (int i = 0; i < kp; i++) xk[i] = xt[SMALL_LEVEL - kp + i];
+#pragma unroll
+  for (int i = 0; i <= k; i++) zk[i] = z[i];
+  mul_regs<kp, k + 1>(xk, zk, v1);
+#pragma unroll
+  for (int i = 0; i < l1; i++) t1[i] = v1[j + i];
+  mul_regs<l1, k + 1>(t1, zk, w);
+  const bool neg = w[L] != 0u;
+#pragma unroll
+  for (int i = 0; i < lt; i++) {
+    const int idx = 2 * k - 1 - j + i;
+    em[i] = (idx < L) ? (neg ? w[idx] : ~w[idx]) : 0u;
+  }
+  mul_regs<k + 1, lt>(zk, em, p);
+  level_update<k, kp, k + 1 + lt, k + 1>(zk, p, 1, neg, z);
+}
+
+// Runs levels lv[1 .. end) (all k' <= SMALL_LEVEL) on the calling lane; v holds level 1's
+// two limbs on entry and the last level's limbs on return.
+template <bool SQRT>
+__device__ __noinline__ void small_levels(const uint32_t (&top)[SMALL_LEVEL], const int *lv, int end,
+                                          uint32_t (&v)[SMALL_LEVEL + 1]) {
+  for (int li = 1; li < end; li++) {
+    switch (lv[li]) {
+#define GFPA_SMALL_LEVEL(K_, KP_) \
+      case KP_: if (SQRT) sqrt_level_regs<K_, KP_>(top, v); else div_level_regs<K_, KP_>(top, v); break;
+      GFPA_SMALL_LEVEL(1, 2) GFPA_SMALL_LEVEL(2, 3) GFPA_SMALL_LEVEL(3, 4) GFPA_SMALL_LEVEL(3, 5)
+      GFPA_SMALL_LEVEL(4, 6) GFPA_SMALL_LEVEL(4, 7) GFPA_SMALL_LEVEL(5, 8) GFPA_SMALL_LEVEL(5, 9)
+#undef GFPA_SMALL_LEVEL
+      default: break;
+    }
+  }
+}
+
+// first level index the group runs: the small ones go to small_levels
+__device__ __forceinline__ int small_levels_end(const int *lv, int nl, bool km) {
+  const int last = km ? nl - 1 : nl;
+  int e = 1;
+  while (e < last && lv[e] <= SMALL_LEVEL) e++;
+  return e;
+}
+
+// ---------------------------------------------------------------------------------------
 // div.  Reference: fpa_warp_div.h:127-201.
 //   1. Y ~ 2^(64n)/B by Newton: Y_k' = Y_k*2^(32(k'-k)) + Y_k*E/2^(64k),
 //      E = 2^(32(k+k')) - B_k' * Y_k   (B_k' = top k' limbs of B).
@@ -463,15 +572,25 @@ __device__ void op_div(const Grp<G> &g, uint32_t *ws, int n, int mode,
   uint32_t *Q = P2 + (2 * N + 8);
   uint32_t *Rm = T;                  // T is dead once Q is formed
   uint32_t *X = P2;                  // P2 (Q*B) is dead once Rm is formed
-  if (g.lane == 0) {
-    uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)b[n - 1];   // level 1: floor((2^64-1)/B_top)
-    Y[0] = (uint32_t)y; Y[1] = (uint32_t)(y >> 32);
-  }
-  g.sync();
   int lv[24];
   const int nl = newton_levels(n, lv);
   const bool km = n >= 4;                      // last level replaced by one Karp-Markstein step
-  for (int li = 1; li < (km ? nl - 1 : nl); li++) {
+  const int l0 = small_levels_end(lv, nl, km);
+  if (g.lane == 0) {
+    uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)b[n - 1];   // level 1: floor((2^64-1)/B_top)
+    uint32_t v[SMALL_LEVEL + 1], bt[SMALL_LEVEL];
+#pragma unroll
+    for (int i = 0; i <= SMALL_LEVEL; i++) v[i] = 0u;
+    v[0] = (uint32_t)y; v[1] = (uint32_t)(y >> 32);
+#pragma unroll
+    for (int i = 0; i < SMALL_LEVEL; i++) bt[i] = (n - SMALL_LEVEL + i >= 0) ? b[n - SMALL_LEVEL + i] : 0u;
+    small_levels<false>(bt, lv, l0, v);
+    const int k = lv[l0 - 1];
+#pragma unroll
+    for (int i = 0; i <= SMALL_LEVEL; i++) if (i <= k) Y[i] = v[i];
+  }
+  g.sync();
+  for (int li = l0; li < (km ? nl - 1 : nl); li++) {
     const int k = lv[li - 1], kp = lv[li];
     const uint32_t *Bk = b + (n - kp);
     // T = B_k' * Y_k   (k' x (k+1) limbs)
@@ -615,17 +734,27 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   const int odd = (int)(e & 1);
   const long long eh = (e + odd) / 2;          // exact: e + odd is even
   grp_copy<G>(g, Xh, Shifted{a, n, 32 - odd}, n + 1);
+  int lv[24];
+  const int nl = newton_levels(n, lv);
+  const bool km = n >= 4;                      // last level replaced by one Karp-Markstein step
+  const int l0 = small_levels_end(lv, nl, km);
   if (g.lane == 0) {
     uint64_t x1 = (uint64_t)Xh[n] << 32;                   // top limb of A_ext, in [2^30, 2^32)
     uint64_t s1 = isqrt64(x1);                             // in [2^31, 2^32)
     uint64_t z = 0xFFFFFFFFFFFFFFFFull / s1;               // level 1: ~ 2^32 / sqrt(x)
-    Z[0] = (uint32_t)z; Z[1] = (uint32_t)(z >> 32);
+    uint32_t v[SMALL_LEVEL + 1], xt[SMALL_LEVEL];
+#pragma unroll
+    for (int i = 0; i <= SMALL_LEVEL; i++) v[i] = 0u;
+    v[0] = (uint32_t)z; v[1] = (uint32_t)(z >> 32);
+#pragma unroll
+    for (int i = 0; i < SMALL_LEVEL; i++) xt[i] = (n + 1 - SMALL_LEVEL + i >= 0) ? Xh[n + 1 - SMALL_LEVEL + i] : 0u;
+    small_levels<true>(xt, lv, l0, v);
+    const int k = lv[l0 - 1];
+#pragma unroll
+    for (int i = 0; i <= SMALL_LEVEL; i++) if (i <= k) Z[i] = v[i];
   }
   g.sync();
-  int lv[24];
-  const int nl = newton_levels(n, lv);
-  const bool km = n >= 4;                      // last level replaced by one Karp-Markstein step
-  for (int li = 1; li < (km ? nl - 1 : nl); li++) {
+  for (int li = l0; li < (km ? nl - 1 : nl); li++) {
     const int k = lv[li - 1], kp = lv[li];
     // V = X_k' Z_k^2 as (X_k' Z_k) Z_k: the low j = k-2 limbs of T1 = X_k' Z_k only reach V
     // below limb 2k-1, the lowest limb of E that is read, so T2 = (T1 >> 32j) Z_k = V / 2^(32j)
