@@ -93,6 +93,8 @@ def lib():
         "fpa_batch_destroy": (i32, [vp]),
         "fpa_gb300_set_op_config": (i32, [i32, u32, i32]),
         "fpa_gb300_get_op_config": (i32, [i32, u32]),
+        "fpa_gb300_set_karatsuba_limbs": (i32, [u32]),
+        "fpa_gb300_get_karatsuba_limbs": (u32, []),
         "fpa_server_create": (i32, [ctypes.POINTER(vp), ctypes.POINTER(ServerConfig)]),
         "fpa_server_submit": (ctypes.c_int64, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp]),
         "fpa_server_wait": (i32, [vp, ctypes.c_int64, ctypes.c_int64]),
@@ -289,6 +291,15 @@ def set_op_config(op, limbs, cfg):
 
 def get_op_config(op, limbs):
     return lib().fpa_gb300_get_op_config(op, limbs)
+
+
+def set_karatsuba_limbs(limbs):
+    """fpa_mul takes one Karatsuba level from `limbs` limbs up (0 = never)."""
+    return lib().fpa_gb300_set_karatsuba_limbs(limbs)
+
+
+def get_karatsuba_limbs():
+    return lib().fpa_gb300_get_karatsuba_limbs()
 
 
 # fpa_gb300.h: fpa_batch_desc (32 bytes)

@@ -6,6 +6,7 @@
 // order (instance-major, little-endian limbs), so copies are plain cudaMemcpy calls with
 // no host-side transpose; CUDA errors are returned as fpa_device_error.
 #include <cuda_runtime.h>
+#include <atomic>
 #include <mutex>
 #include <string.h>
 #include "../../include/fpa.h"
@@ -75,6 +76,9 @@ bool valid_precision(uint32_t precision) {
 }
 
 
+// mul: Karatsuba split from this many limbs (0xFFFFFFFF = never)
+static std::atomic<uint32_t> g_kara_min{GFPA_KARATSUBA_DEFAULT};
+
 fpa_result launch_elementwise(int op, uint32_t precision, uint64_t count, int mode, uint32_t *r_exps, uint32_t *r_limbs,
                               const uint32_t *a_exps, const uint32_t *a_limbs, const uint32_t *b_exps,
                               const uint32_t *b_limbs, cudaStream_t stream) {
@@ -89,6 +93,7 @@ fpa_result launch_elementwise(int op, uint32_t precision, uint64_t count, int mo
   args.a_exps = a_exps; args.a_limbs = a_limbs;
   args.b_exps = (op == 4) ? a_exps : b_exps; args.b_limbs = (op == 4) ? a_limbs : b_limbs;
   args.err = err;
+  if (op == 2) args.kara_min = g_kara_min.load(std::memory_order_relaxed);
   int cfg = gfpa_cfg_for_op(op, args.n);
   if (cfg < 0) return fpa_invalid_precisions;
   return gfpa_launch(cfg, op, &args, stream, sms) == cudaSuccess ? fpa_success : fpa_device_error;
@@ -322,6 +327,16 @@ fpa_result fpa_gb300_set_config(uint32_t limbs, int cfg) {
 }
 
 int fpa_gb300_get_config(uint32_t limbs) { return gfpa_cfg_for_op(2, limbs); }
+
+fpa_result fpa_gb300_set_karatsuba_limbs(uint32_t limbs) {
+  g_kara_min.store(limbs == 0 ? 0xFFFFFFFFu : limbs, std::memory_order_relaxed);
+  return fpa_success;
+}
+
+uint32_t fpa_gb300_get_karatsuba_limbs(void) {
+  const uint32_t v = g_kara_min.load(std::memory_order_relaxed);
+  return v == 0xFFFFFFFFu ? 0u : v;
+}
 
 const char *fpa_gb300_version(void) { return "fpa_gb300 0.1 (sm_103a)"; }
 

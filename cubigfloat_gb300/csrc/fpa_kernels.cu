@@ -142,7 +142,8 @@ __device__ __forceinline__ void addsub_pipelined(const Grp<G> &g, uint32_t *ws, 
 
 // mul: the same double buffering; the zero padding around the staged operands is the same
 // for every operation of a launch, so it is written once.
-template <int G, int K, int R>
+// KARA: the instantiation with the Karatsuba split (launched from its threshold up).
+template <int G, int K, int R, bool KARA>
 __device__ __forceinline__ void mul_pipelined(const Grp<G> &g, uint32_t *ws, const ElementwiseArgs &args, uint64_t i,
                                               uint64_t stride) {
   constexpr int N = G * K * R;
@@ -152,6 +153,7 @@ __device__ __forceinline__ void mul_pipelined(const Grp<G> &g, uint32_t *ws, con
   uint32_t *P = ws + MulScratch<G, K, R>::words();
   uint32_t *xa[2] = {s.sa, P + 2 * N + 4};
   uint32_t *yb[2] = {s.sb, xa[1] + N};
+  uint32_t *kws = KARA ? yb[1] + N + 2 * K : nullptr;   // Karatsuba staging
   for (int j = g.lane; j < NK; j += G)
     if (j >= n) { xa[0][j] = 0u; xa[1][j] = 0u; }
   for (int j = g.lane; j < NK + 2 * K; j += G)
@@ -178,7 +180,7 @@ __device__ __forceinline__ void mul_pipelined(const Grp<G> &g, uint32_t *ws, con
     cp_async_wait<1>();                          // this operation's operands have landed
     g.sync();
     s.sa = xa[cur]; s.sb = yb[cur];
-    op_mul_staged<G, K, R>(g, s, P, n, args.mode, ae, be, args.r_exps + i, args.r_limbs + i * n);
+    op_mul_staged<G, K, R>(g, s, P, n, args.mode, ae, be, args.r_exps + i, args.r_limbs + i * n, kws);
     g.sync();                                    // the buffer is refilled two operations on
     ae = nae; be = nbe; cur ^= 1;
   }
@@ -196,8 +198,9 @@ __global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(Elemen
     addsub_pipelined<OP, G, K, R>(g, ws, args, (uint64_t)blockIdx.x * gpc + gi, (uint64_t)gridDim.x * gpc);
     return;
   }
-  if constexpr (OP == OP_MUL) {
-    mul_pipelined<G, K, R>(g, ws, args, (uint64_t)blockIdx.x * gpc + gi, (uint64_t)gridDim.x * gpc);
+  if constexpr (OP == OP_MUL || OP == OP_MUL_KARA) {
+    mul_pipelined<G, K, R, OP == OP_MUL_KARA>(g, ws, args, (uint64_t)blockIdx.x * gpc + gi,
+                                               (uint64_t)gridDim.x * gpc);
     return;
   }
   for (uint64_t i = (uint64_t)blockIdx.x * gpc + gi; i < args.count; i += (uint64_t)gridDim.x * gpc) {
@@ -227,6 +230,9 @@ static cudaError_t launch_op(const ElementwiseArgs &args, cudaStream_t stream, i
   constexpr int G = CFG_G, K = CFG_K, R = CFG_R;
   if constexpr (OP == OP_ADD || OP == OP_SUB) {
     if ((int)args.n <= G * K) return launch_addsub_regk<OP, G, K>(args, stream, sms);
+  }
+  if constexpr (OP == OP_MUL && KaratsubaCfg<G, K, R>::on) {
+    if (args.n >= 4 && args.n >= args.kara_min) return launch_op<OP_MUL_KARA>(args, stream, sms);
   }
   constexpr size_t warp_bytes = (size_t)(32 / G) * Words<OP, G, K, R>::aligned() * sizeof(uint32_t);
   constexpr size_t cta_max = 227 * 1024;

@@ -17,12 +17,16 @@ struct ElementwiseArgs {
   const uint32_t *b_exps, *b_limbs;
   uint32_t *err;
   const uint32_t *c_exps = nullptr, *c_limbs = nullptr;   // third operand (fma only)
+  uint32_t kara_min = 0xFFFFFFFFu;   // mul: Karatsuba split from this many limbs (tile >= 8)
 };
 
 #define GFPA_NUM_CFGS 18
 #define GFPA_OP_FMA 5        // elementwise operation code of fma (after add, sub, mul, div, sqrt)
 #define GFPA_NUM_DEFAULT_CFGS 7
 #define GFPA_MAX_LIMBS 512
+#ifndef GFPA_KARATSUBA_DEFAULT
+#define GFPA_KARATSUBA_DEFAULT 0xFFFFFFFFu   // mul: Karatsuba split from this many limbs
+#endif
 
 // Lane-group configurations (G lanes x K limbs per tile x R block pairs per lane, capacity
 // G*K*R limbs).  0..6 are the defaults in increasing capacity; 7..15 put two to eight

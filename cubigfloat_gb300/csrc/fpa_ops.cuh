@@ -10,6 +10,12 @@
 
 namespace gfpa {
 
+// Configurations that carry the Karatsuba split of mul, and the elementwise kernel
+// instantiation that runs it (an operation code of the kernels only).
+template <int G, int K, int R>
+struct KaratsubaCfg { static constexpr bool on = K >= 8 && G * K * R >= 256; };
+constexpr int OP_MUL_KARA = 6;
+
 // Workspace words per group, beyond MulScratch.  N = G*K*R is the group's limb capacity.
 template <int G, int K, int R>
 struct OpSpace {
@@ -32,7 +38,7 @@ template <int OP, int G, int K, int R>
 struct OpWords {
   __host__ __device__ static constexpr int v() {
     return (OP == OP_ADD || OP == OP_SUB) ? OpSpace<G, K, R>::addsub()
-           : MulScratch<G, K, R>::words() + (OP == OP_MUL ? OpSpace<G, K, R>::mul()
+           : MulScratch<G, K, R>::words() + ((OP == OP_MUL || OP == OP_MUL_KARA) ? OpSpace<G, K, R>::mul()
                                           : OP == OP_DIV ? OpSpace<G, K, R>::div()
                                           : OP == OP_SQRT ? OpSpace<G, K, R>::sqrt() : OpSpace<G, K, R>::fma());
   }
@@ -40,12 +46,14 @@ struct OpWords {
 };
 
 // The elementwise kernels double-buffer the operands of add/sub and mul (the next
-// operation's copies are in flight while the group computes): one more staged pair each.
+// operation's copies are in flight while the group computes): one more staged pair each;
+// the Karatsuba mul instantiation also carries the split's staging (N + K words).
 template <int OP, int G, int K, int R>
 struct PipeWords {
   static constexpr int N = G * K * R;
   __host__ __device__ static constexpr int v() {
-    return OpWords<OP, G, K, R>::v() + ((OP == OP_ADD || OP == OP_SUB) ? 2 * N : (OP == OP_MUL ? 2 * N + 2 * K : 0));
+    return OpWords<OP, G, K, R>::v() + ((OP == OP_ADD || OP == OP_SUB) ? 2 * N
+                                        : OP == OP_MUL ? 2 * N + 2 * K : (OP == OP_MUL_KARA ? 3 * N + 3 * K : 0));
   }
   __host__ __device__ static constexpr int aligned() { return (v() + 3) & ~3; }
 };
@@ -286,15 +294,67 @@ __device__ void op_addsub_reg(const Grp<G> &g, int n, int mode, int is_sub, uint
 }
 
 // ---------------------------------------------------------------------------------------
+// Karatsuba split of a staged square product (x in s.sa, y in s.sb + K, n limbs each):
+//   P[0..2n) = z0 + z1 2^(32h) + z2 2^(64h),  h = ceil(n/2),
+//   z0 = x0 y0,  z2 = x1 y1,  z1 = (x0 + x1)(y0 + y1) - z0 - z2.
+// The three half products run on tiles of K/2 limbs, so all G lanes stay busy on h limbs
+// (with K-limb tiles half of them would idle).  The sums x0 + x1 = cx 2^(32h) + sx and
+// y0 + y1 = cy 2^(32h) + sy are kept to h limbs: cx sy + cy sx + cx cy 2^(32h) is added
+// at 2^(32h) afterwards, so every half product is h x h.  kws: N + K words (the half
+// products' staging); z1 is formed in s.sb once x and y have been read, and s.sb's low K
+// zero limbs are restored at the end.
+template <int G, int K, int R>
+__device__ __noinline__ void grp_mul_karatsuba(const Grp<G> g, uint32_t *P, int n, const MulScratch<G, K, R> s,
+                                               uint32_t *kws) {
+  constexpr int KS = K / 2, N = G * K * R;
+  static_assert(KS >= 4, "Karatsuba halves use tiles of at least 4 limbs");
+  MulScratch<G, KS, R> s2;
+  s2.sa = kws; s2.sb = kws + N / 2; s2.snap = s.snap; s2.ov = s.ov;
+  const int h = (n + 1) / 2, u = n - h;
+  const uint32_t *x = s.sa, *y = s.sb + K;
+  grp_mul<G, KS, R>(g, P, Ptr{x, h}, h, Ptr{y, h}, h, s2);                    // z0 -> P[0, 2h)
+  grp_mul<G, KS, R>(g, P + 2 * h, Ptr{x + h, u}, u, Ptr{y + h, u}, u, s2);    // z2 -> P[2h, 2n)
+  // sx, sy staged in place for the middle product (KS zero limbs below sy, zeros above both)
+  const uint32_t cx = grp_add<G>(g, s2.sa, Ptr{x, h}, Ptr{x + h, u}, h, 0u);
+  const uint32_t cy = grp_add<G>(g, s2.sb + KS, Ptr{y, h}, Ptr{y + h, u}, h, 0u);
+  const int M = (h + KS - 1) / KS;
+  for (int i = g.lane; i < M * KS + 2 * KS; i += G) {
+    if (i >= h && i < M * KS) s2.sa[i] = 0u;
+    if (i < KS || i >= KS + h) s2.sb[i] = 0u;
+  }
+  g.sync();
+  uint32_t *Z1 = s.sb;                                                         // 2h+2 <= n+3 limbs
+  grp_mul_call<G, KS, R>(g, Z1, h, h, s2);                                     // sx sy -> Z1[0, 2h)
+  if (g.lane == 0) { Z1[2 * h] = cx & cy; Z1[2 * h + 1] = 0u; }
+  g.sync();
+  if (cx) grp_add<G>(g, Z1 + h, Ptr{Z1 + h, h + 2}, Ptr{s2.sb + KS, h}, h + 2, 0u);
+  if (cy) grp_add<G>(g, Z1 + h, Ptr{Z1 + h, h + 2}, Ptr{s2.sa, h}, h + 2, 0u);
+  grp_sub<G>(g, Z1, Ptr{Z1, 2 * h + 2}, Ptr{P, 2 * h}, 2 * h + 2, 0u);          // - z0
+  grp_sub<G>(g, Z1, Ptr{Z1, 2 * h + 2}, Ptr{P + 2 * h, 2 * u}, 2 * h + 2, 0u);  // - z2
+  grp_add<G>(g, P + h, Ptr{P + h, 2 * n - h}, Ptr{Z1, 2 * h + 2}, 2 * n - h, 0u);
+  for (int i = g.lane; i < K; i += G) s.sb[i] = 0u;
+  g.sync();
+}
+
+// ---------------------------------------------------------------------------------------
 // mul.  Reference: fpa_warp_mul.h:41-139.  Exact 2n-limb product, one rounding.
 // Range (:124-128): TINY when BIAS+e < 5, INF when BIAS+e > 0x7FFFFFFF.
+// kws != nullptr: the product takes the Karatsuba split (N + K words of staging), compiled
+// into the configurations that hold at least 256 limbs on tiles of at least 8 limbs (the
+// split only pays at large sizes; out of line so that the schoolbook path keeps its
+// registers).
 template <int G, int K, int R>
 __device__ __forceinline__ void op_mul_staged(const Grp<G> &g, const MulScratch<G, K, R> &s, uint32_t *P, int n,
                                               int mode, uint32_t a_exp, uint32_t b_exp, uint32_t *r_exp,
-                                              uint32_t *r) {
+                                              uint32_t *r, uint32_t *kws = nullptr) {
   const uint32_t act = c_action[2][classify(a_exp) * 9 + classify(b_exp)];
   if (act != ACT_MUL) { write_class<G>(g, r_exp, act); return; }
-  grp_mulsq_staged<G, K, R>(g, P, n, s);
+  if constexpr (KaratsubaCfg<G, K, R>::on) {
+    if (kws) grp_mul_karatsuba<G, K, R>(g, P, n, s, kws);
+    else grp_mulsq_staged<G, K, R>(g, P, n, s);
+  } else {
+    grp_mulsq_staged<G, K, R>(g, P, n, s);
+  }
   const uint32_t sign = (a_exp ^ b_exp) & 1u;
   Rounded res;
   grp_round<G>(g, P, 2 * n, n, 0u, mode, sign, res);

@@ -171,6 +171,15 @@ fpa_result fpa_gb300_autotune(fpa_op op, uint32_t limbs, uint32_t sample, int *b
  * environment variable FPA_GB300_TUNING) when it is loaded. */
 fpa_result fpa_gb300_load_tuning(const char *path);
 
+/* Karatsuba split for fpa_mul (and the mul launches of fpa_gb300_elementwise): numbers of at
+ * least `limbs` limbs whose configuration holds at least 256 limbs on tiles of at least
+ * 8 limbs take one Karatsuba level (three half-size products) instead of the schoolbook
+ * product; 0 = never.  The
+ * result is the same either way (the product is exact).  The default is the threshold
+ * measured fastest on GB300. */
+fpa_result fpa_gb300_set_karatsuba_limbs(uint32_t limbs);
+uint32_t fpa_gb300_get_karatsuba_limbs(void);
+
 /* Measured integer multiply-add throughput of the current GPU (mad.lo.u32 and mad.hi.u32
  * per second over all SMs): the roofline denominator for the multiply-bound operations. */
 fpa_result fpa_gb300_measure_imad_peak(double *mad_lo_per_s, double *mad_hi_per_s);
