@@ -32,8 +32,8 @@ struct ElementwiseArgs {
 // G*K*R limbs).  0..6 are the defaults in increasing capacity; 7..15 put two to eight
 // operations in one warp (fewer lanes per operation, wider tiles or several block pairs
 // per lane), which the autotuner can choose (mostly for div/sqrt); 16 and 17 run add/sub
-// only, on groups of four lanes holding 8 or 16 limbs each in registers
-// (fpa_addsub_narrow.cu).
+// only (fpa_addsub_narrow.cu): 16 one thread per operation on shared-memory rows for 8, 16
+// and 32 limbs and four lanes x 8 limbs otherwise, 17 four lanes x 16 limbs in registers.
 static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4, 4, 4};
 static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4, 8, 16};
 static const int gfpa_cfg_R[GFPA_NUM_CFGS] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 2, 4, 2, 8, 1, 1};

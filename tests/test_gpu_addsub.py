@@ -79,7 +79,7 @@ def sizes_for(cfg):
     lanes, tile, pairs = fpa.configs()[cfg]
     gk = lanes * tile
     cap = gk * pairs
-    out = {1, 2, 3, 4, 5, gk // 2, gk // 2 + 1, gk - 1, gk, gk + 1, cap - 1, cap}
+    out = {1, 2, 3, 4, 5, 8, 16, gk // 2, gk // 2 + 1, gk - 1, gk, gk + 1, cap - 1, cap}
     return sorted(x for x in out if 1 <= x <= min(cap, 512))
 
 
