@@ -203,25 +203,31 @@ __global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(Elemen
                                                (uint64_t)gridDim.x * gpc);
     return;
   }
-  for (uint64_t i = (uint64_t)blockIdx.x * gpc + gi; i < args.count; i += (uint64_t)gridDim.x * gpc) {
-    const uint64_t off = i * (uint64_t)n;
-    const uint32_t a_exp = args.a_exps[i];
-    const uint32_t b_exp = (OP == OP_SQRT) ? 0u : args.b_exps[i];
-    if (OP == OP_ADD || OP == OP_SUB)
-      op_addsub<G, K, R>(g, ws, n, args.mode, OP == OP_SUB, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
-                      args.r_exps + i, args.r_limbs + off);
-    else if (OP == OP_MUL)
-      op_mul<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
-                   args.r_exps + i, args.r_limbs + off);
-    else if (OP == OP_DIV)
-      op_div<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
-                   args.r_exps + i, args.r_limbs + off, args.err);
-    else if (OP == OP_SQRT)
-      op_sqrt<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, args.r_exps + i, args.r_limbs + off, args.err);
-    else
-      op_fma<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off, args.c_exps[i],
-                      args.c_limbs + off, args.r_exps + i, args.r_limbs + off);
-    g.sync();   // the group's shared slice is reused by its next instance
+  // div / sqrt / fma.  Every thread of the CTA runs the same number of iterations and meets
+  // a CTA barrier after each: the warps then go through an operation's phases together and
+  // share the fetched code of each phase (div and sqrt are 130-190 KB of code, and with the
+  // warps spread over the phases instruction-fetch stalls led; measured on 8x4x4 at 4096
+  // bits: div +16 %, sqrt +8 %).
+  const uint64_t total = (uint64_t)gridDim.x * gpc;
+  const uint64_t iters = (args.count + total - 1) / total;
+  for (uint64_t it = 0; it < iters; it++) {
+    const uint64_t i = it * total + (uint64_t)blockIdx.x * gpc + gi;
+    if (i < args.count) {
+      const uint64_t off = i * (uint64_t)n;
+      const uint32_t a_exp = args.a_exps[i];
+      const uint32_t b_exp = (OP == OP_SQRT) ? 0u : args.b_exps[i];
+      if (OP == OP_DIV)
+        op_div<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off,
+                        args.r_exps + i, args.r_limbs + off, args.err);
+      else if (OP == OP_SQRT)
+        op_sqrt<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, args.r_exps + i, args.r_limbs + off,
+                         args.err);
+      else
+        op_fma<G, K, R>(g, ws, n, args.mode, a_exp, args.a_limbs + off, b_exp, args.b_limbs + off, args.c_exps[i],
+                        args.c_limbs + off, args.r_exps + i, args.r_limbs + off);
+      g.sync();   // the group's shared slice is reused by its next instance
+    }
+    __syncthreads();
   }
 }
 
