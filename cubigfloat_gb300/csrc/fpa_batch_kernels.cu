@@ -25,22 +25,31 @@ __device__ __noinline__ void run_task(const BatchArgs A, uint32_t first, uint32_
   const int gi = (int)((threadIdx.x & 31u) / G);
   uint32_t *ws = smem + (size_t)warp * A.warp_words + gi * words;
   const int stride = nwarps * gpw;
-  for (uint32_t j = (uint32_t)(warp * gpw + gi); j < count; j += stride) {
-    const uint32_t idx = A.order[first + j];
-    const fpa_batch_desc d = A.descs[idx];
-    const int n = d.limbs, mode = d.mode;
-    if (OP == OP_ADD || OP == OP_SUB)
-      op_addsub<G, K, R>(g, ws, n, mode, OP == OP_SUB, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx],
-                      A.b_limbs + d.b_off, A.r_exps + idx, A.r_limbs + d.r_off);
-    else if (OP == OP_MUL)
-      op_mul<G, K, R>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx], A.b_limbs + d.b_off,
-                   A.r_exps + idx, A.r_limbs + d.r_off);
-    else if (OP == OP_DIV)
-      op_div<G, K, R>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx], A.b_limbs + d.b_off,
-                   A.r_exps + idx, A.r_limbs + d.r_off, A.err);
-    else
-      op_sqrt<G, K, R>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.r_exps + idx, A.r_limbs + d.r_off, A.err);
-    g.sync();
+  // div / sqrt: every thread of the CTA (all on this task) runs the same number of
+  // iterations and meets a CTA barrier after each, so the warps share the fetched code of
+  // each phase (as in the elementwise kernel).  The barrier has one call site, after the
+  // per-group branch: a warp's lanes must all reach the same barrier instruction.
+  constexpr bool lockstep = OP == OP_DIV || OP == OP_SQRT;
+  const uint32_t iters = lockstep ? (count + stride - 1) / stride : 0u;
+  for (uint32_t it = 0, j = (uint32_t)(warp * gpw + gi); lockstep ? it < iters : j < count; it++, j += stride) {
+    if (j < count) {
+      const uint32_t idx = A.order[first + j];
+      const fpa_batch_desc d = A.descs[idx];
+      const int n = d.limbs, mode = d.mode;
+      if (OP == OP_ADD || OP == OP_SUB)
+        op_addsub<G, K, R>(g, ws, n, mode, OP == OP_SUB, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx],
+                        A.b_limbs + d.b_off, A.r_exps + idx, A.r_limbs + d.r_off);
+      else if (OP == OP_MUL)
+        op_mul<G, K, R>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx], A.b_limbs + d.b_off,
+                     A.r_exps + idx, A.r_limbs + d.r_off);
+      else if (OP == OP_DIV)
+        op_div<G, K, R>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.b_exps[idx], A.b_limbs + d.b_off,
+                     A.r_exps + idx, A.r_limbs + d.r_off, A.err);
+      else
+        op_sqrt<G, K, R>(g, ws, n, mode, A.a_exps[idx], A.a_limbs + d.a_off, A.r_exps + idx, A.r_limbs + d.r_off, A.err);
+      g.sync();
+    }
+    if (lockstep) __syncthreads();
   }
 }
 

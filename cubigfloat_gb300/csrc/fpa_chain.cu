@@ -79,24 +79,38 @@ __global__ void __launch_bounds__(128, 4) k_newton_sqrt(ChainArgs A) {
   uint32_t *ws = smem + gi * W;
   uint32_t *y = ws + ChainSpace<G, K, R>::ws_newton, *t = y + V, *s = t + V;
   const int n = (int)A.n;
-  for (uint64_t d = (uint64_t)blockIdx.x * gpc + gi; d < A.count; d += (uint64_t)gridDim.x * gpc) {
+  // every thread of the CTA runs the same number of iterations and meets a CTA barrier after
+  // each Newton step, so the warps go through the division's phases together (shared
+  // instruction fetch, as in the elementwise div kernel)
+  const uint64_t total = (uint64_t)gridDim.x * gpc, rounds = (A.count + total - 1) / total;
+  for (uint64_t q = 0; q < rounds; q++) {
+    const uint64_t d = q * total + (uint64_t)blockIdx.x * gpc + gi;
+    const bool act = d < A.count;
     const uint64_t off = d * (uint64_t)n;
-    for (int i = g.lane; i < n; i += G) y[4 + i] = A.y_limbs[off + i];
-    if (g.lane == 0) y[0] = A.y_exps[d];
-    g.sync();
-    const uint32_t xe = A.x_exps[d];
+    uint32_t xe = 0;
+    if (act) {
+      for (int i = g.lane; i < n; i += G) y[4 + i] = A.y_limbs[off + i];
+      if (g.lane == 0) y[0] = A.y_exps[d];
+      g.sync();
+      xe = A.x_exps[d];
+    }
     for (uint32_t it = 0; it < A.len; it++) {
-      op_div<G, K, R>(g, ws, n, A.mode, xe, A.x_limbs + off, y[0], y + 4, t, t + 4, A.err);      // t = x / y
-      g.sync();
-      op_addsub<G, K, R>(g, ws, n, A.mode, 0, y[0], y + 4, t[0], t + 4, s, s + 4);             // s = y + t
-      g.sync();
-      for (int i = g.lane; i < n; i += G) y[4 + i] = s[4 + i];                              // y = s * 0.5
-      if (g.lane == 0) y[0] = half_of(s[0]);
+      if (act) {
+        op_div<G, K, R>(g, ws, n, A.mode, xe, A.x_limbs + off, y[0], y + 4, t, t + 4, A.err);    // t = x / y
+        g.sync();
+        op_addsub<G, K, R>(g, ws, n, A.mode, 0, y[0], y + 4, t[0], t + 4, s, s + 4);           // s = y + t
+        g.sync();
+        for (int i = g.lane; i < n; i += G) y[4 + i] = s[4 + i];                            // y = s * 0.5
+        if (g.lane == 0) y[0] = half_of(s[0]);
+        g.sync();
+      }
+      __syncthreads();
+    }
+    if (act) {
+      for (int i = g.lane; i < n; i += G) A.r_limbs[off + i] = y[4 + i];
+      if (g.lane == 0) A.r_exps[d] = y[0];
       g.sync();
     }
-    for (int i = g.lane; i < n; i += G) A.r_limbs[off + i] = y[4 + i];
-    if (g.lane == 0) A.r_exps[d] = y[0];
-    g.sync();
   }
 }
 
