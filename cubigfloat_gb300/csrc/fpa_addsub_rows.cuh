@@ -1,5 +1,5 @@
-// fpa_addsub_rows.cuh -- add/sub with one thread per operation on shared-memory rows, for
-// numbers of exactly N = 8, 16 or 32 limbs (256, 512 and 1024 bits).
+// fpa_addsub_rows.cuh -- add/sub and mul with one thread per operation on shared-memory
+// rows, for numbers of exactly N = 8, 16 or 32 limbs (256, 512 and 1024 bits).
 //
 // A lane group repeats an operation's scalar work (classes, exponents, the rounding
 // decision) on every lane, which leaves a few-hundred-bit add/sub bound by integer issue,
@@ -160,6 +160,61 @@ __device__ __forceinline__ uint32_t row_addsub(uint32_t *ra, const uint32_t *rb,
   return (uint32_t)(2 * be) + sign;
 }
 
+// mul of two rows by one thread: product scanning over the 2N-1 columns with a 96-bit
+// (lo, hi, top) accumulator and compile-time indices; the limbs below the top N+2 of the
+// product only feed the sticky bit.  The product of two normalised mantissas has its top
+// bit at 64N-1 or 64N-2, so the mantissa is the top N limbs shifted by 0 or 1 bit.
+// Reference: fpa_warp_mul.h:41-139 (one rounding; TINY when BIAS+e < 5, INF when
+// BIAS+e > 0x7FFFFFFF, :124-128).
+template <int N>
+__device__ __forceinline__ uint32_t row_mul(uint32_t *ra, const uint32_t *rb, uint32_t a_exp, uint32_t b_exp,
+                                            int mode) {
+  const uint32_t act = c_action[2][classify(a_exp) * 9 + classify(b_exp)];
+  if (act != ACT_MUL) return act;
+  uint32_t a[N], b[N];
+#pragma unroll
+  for (int s = 0; s < N; s += 4) {
+    const uint4 u = *reinterpret_cast<const uint4 *>(ra + s), v = *reinterpret_cast<const uint4 *>(rb + s);
+    a[s] = u.x; a[s + 1] = u.y; a[s + 2] = u.z; a[s + 3] = u.w;
+    b[s] = v.x; b[s + 1] = v.y; b[s + 2] = v.z; b[s + 3] = v.w;
+  }
+  uint32_t top[N + 2], low = 0, lo = 0, hi = 0, tp = 0;   // top[k] = product limb N-2+k
+#pragma unroll
+  for (int c = 0; c < 2 * N - 1; c++) {
+#pragma unroll
+    for (int i = (c < N ? 0 : c - N + 1); i <= (c < N ? c : N - 1); i++) mac3(lo, hi, tp, a[i], b[c - i]);
+    if (c < N - 2) low |= lo;
+    else top[c - (N - 2)] = lo;
+    lo = hi; hi = tp; tp = 0;
+  }
+  top[N + 1] = lo;                                          // limb 2N-1
+  const uint32_t sign = (a_exp ^ b_exp) & 1u;
+  const bool full = (top[N + 1] >> 31) != 0u;               // top bit at 64N-1
+  uint32_t mant[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) mant[i] = full ? top[i + 2] : ((top[i + 2] << 1) | (top[i + 1] >> 31));
+  // round bit: product bit 32N-1 (full) or 32N-2; sticky: everything below it
+  const uint32_t rl = top[1];                               // limb N-1
+  const uint32_t rbit = full ? (rl >> 31) : ((rl >> 30) & 1u);
+  const uint32_t st = ((full ? (rl & 0x7FFFFFFFu) : (rl & 0x3FFFFFFFu)) | top[0] | low) != 0u ? 1u : 0u;
+  uint32_t cy = round_up(mode, sign, mant[0] & 1u, rbit, st) ? 1u : 0u;
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    const uint32_t v = mant[i] + cy;
+    cy = (cy && v == 0u) ? 1u : 0u;
+    mant[i] = v;
+  }
+  if (cy) mant[N - 1] = 0x80000000u;                        // 0.11..1 + ulp = 1.0
+  const int L = full ? 64 * N : 64 * N - 1;
+  const long long e = (long long)(a_exp >> 1) + (long long)(b_exp >> 1) - 2LL * BIAS - 64LL * N + L + (int)cy;
+  if ((long long)BIAS + e < 5) return CLS_POS_TINY - sign;
+  if ((long long)BIAS + e > 0x7FFFFFFFLL) return CLS_POS_INF - sign;
+#pragma unroll
+  for (int s = 0; s < N; s += 4)
+    *reinterpret_cast<uint4 *>(ra + s) = make_uint4(mant[s], mant[s + 1], mant[s + 2], mant[s + 3]);
+  return exp_word(e, sign);
+}
+
 // Copies of one warp's 32 operations from index `base` (cnt of them): limbs of a and b into
 // rows, exponents beside them.  Unit u of the contiguous limbs is chunk r of operation o;
 // (o, r) advance by 32 units per step without a division.
@@ -195,7 +250,7 @@ __device__ __forceinline__ void rows_stage(uint32_t *buf, const ElementwiseArgs 
 }
 
 template <int OP, int N>
-__global__ void __launch_bounds__(128, 4) k_addsub_rows(ElementwiseArgs args) {
+__global__ void __launch_bounds__(128, 4) k_rows(ElementwiseArgs args) {
   extern __shared__ __align__(16) uint32_t smem[];
   constexpr int S = RowSpace<N>::S;
   const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
@@ -221,7 +276,8 @@ __global__ void __launch_bounds__(128, 4) k_addsub_rows(ElementwiseArgs args) {
     const int cnt = (int)min((uint64_t)32, args.count - base);
     uint32_t rexp = 0;
     if (lane < cnt) {
-      rexp = row_addsub<N>(ra + lane * S, rb + lane * S, ea[lane], eb[lane], args.mode, OP == OP_SUB);
+      rexp = OP == OP_MUL ? row_mul<N>(ra + lane * S, rb + lane * S, ea[lane], eb[lane], args.mode)
+                          : row_addsub<N>(ra + lane * S, rb + lane * S, ea[lane], eb[lane], args.mode, OP == OP_SUB);
       args.r_exps[base + lane] = rexp;
     }
     ea[lane] = rexp;                                             // read back by the copy-out below
@@ -253,11 +309,11 @@ __global__ void __launch_bounds__(128, 4) k_addsub_rows(ElementwiseArgs args) {
 }
 
 template <int OP, int N>
-static cudaError_t launch_addsub_rows(const ElementwiseArgs &args, cudaStream_t stream, int sms) {
+static cudaError_t launch_rows(const ElementwiseArgs &args, cudaStream_t stream, int sms) {
   constexpr int warps = 4;
   constexpr size_t smem = (size_t)warps * RowSpace<N>::words * sizeof(uint32_t);
   static int per_sm = 0;
-  auto kern = k_addsub_rows<OP, N>;
+  auto kern = k_rows<OP, N>;
   if (per_sm == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

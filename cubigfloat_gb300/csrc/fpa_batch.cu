@@ -77,11 +77,11 @@ int gfpa_batch_cfg_for(int op, uint32_t n) {
   // A class kernel's CTAs all carry the largest shared-memory slice among its tasks, so one
   // configuration with a large slice lowers the occupancy of every task in its class.  The
   // elementwise table's choice is kept only while a warp's slice leaves room for three CTAs
-  // of its class on an SM; otherwise (and for the add/sub-only configurations, which have
-  // their own elementwise kernel only) the default configuration is used.
+  // of its class on an SM; otherwise (and for configurations 16 and 17, which have
+  // elementwise kernels only) the default configuration is used.
   const int dflt = gfpa_default_cfg(n < 4 ? 4 : n);
   const size_t budget = (227 * 1024 / 3) / (size_t)(gfpa_class_threads[gfpa_class_of(cfg, op)] / 32);
-  if (gfpa_cfg_addsub_only(cfg) || (size_t)warp_words_for(cfg, op) * 4 > budget) return dflt;
+  if (gfpa_cfg_elementwise_only(cfg) || (size_t)warp_words_for(cfg, op) * 4 > budget) return dflt;
   return cfg;
 }
 double gfpa_batch_op_weight(int op, int n) { return op_weight(op, n); }

@@ -31,16 +31,17 @@ struct ElementwiseArgs {
 // Lane-group configurations (G lanes x K limbs per tile x R block pairs per lane, capacity
 // G*K*R limbs).  0..6 are the defaults in increasing capacity; 7..15 put two to eight
 // operations in one warp (fewer lanes per operation, wider tiles or several block pairs
-// per lane), which the autotuner can choose (mostly for div/sqrt); 16 and 17 run add/sub
-// only (fpa_addsub_narrow.cu): 16 one thread per operation on shared-memory rows for 8, 16
-// and 32 limbs and four lanes x 8 limbs otherwise, 17 four lanes x 16 limbs in registers.
+// per lane), which the autotuner can choose (mostly for div/sqrt); 16 and 17 are elementwise
+// only (fpa_addsub_narrow.cu): 16 runs add/sub and mul, one thread per operation on
+// shared-memory rows for 8, 16 and 32 limbs and lane groups otherwise; 17 runs add/sub on
+// four lanes x 16 limbs in registers.
 static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4, 4, 4};
 static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4, 8, 16};
 static const int gfpa_cfg_R[GFPA_NUM_CFGS] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 2, 4, 2, 8, 1, 1};
 static inline int gfpa_cfg_capacity(int c) { return gfpa_cfg_G[c] * gfpa_cfg_K[c] * gfpa_cfg_R[c]; }
-// configurations 16 and 17 run add/sub only
-static inline bool gfpa_cfg_addsub_only(int c) { return c >= 16; }
-static inline bool gfpa_cfg_supports(int c, int op) { return !gfpa_cfg_addsub_only(c) || op <= 1; }
+// configurations 16 (add/sub/mul) and 17 (add/sub) have elementwise kernels only
+static inline bool gfpa_cfg_elementwise_only(int c) { return c >= 16; }
+static inline bool gfpa_cfg_supports(int c, int op) { return c < 16 || op <= 1 || (c == 16 && op == 2); }
 
 extern "C" {
 cudaError_t gfpa_launch_cfg0(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);

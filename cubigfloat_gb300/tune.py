@@ -25,9 +25,9 @@ def tune(sample=1 << 17, ops=range(5), grid=GRID, log=print):
     table = []
     for op in ops:
         prev = 0
-        # add/sub: configuration 16 has kernels for exactly 8, 16 and 32 limbs, so the sizes
-        # just below them get grid points of their own
-        for n in (sorted(set(grid) | {7, 15, 31}) if op in (0, 1) else grid):
+        # add/sub/mul: configuration 16 has kernels for exactly 8, 16 and 32 limbs, so the
+        # sizes just below them get grid points of their own
+        for n in (sorted(set(grid) | {7, 15, 31}) if op in (0, 1, 2) else grid):
             best, rate = ctypes.c_int(-1), ctypes.c_double(0)
             s = sample if n <= 64 else max(4096, sample * 64 // n)       # about the same limbs per point
             if op in (0, 1):       # add/sub are bound by HBM: operands and results well beyond L2

@@ -126,7 +126,7 @@ def test_every_configuration(cfg):
         ae, al = W.uniform(rng, 64, n, -200, 200)
         be, bl = W.uniform(rng, 64, n, -200, 200)
         for op in range(5):
-            if cfg >= 16 and op > 1:               # configurations 16 and 17 run add/sub only
+            if cfg >= 16 and op > (2 if cfg == 16 else 1):    # 16: add/sub/mul, 17: add/sub
                 assert fpa.set_op_config(op, n, cfg) != 0
                 continue
             assert fpa.set_op_config(op, n, cfg) == 0
