@@ -187,8 +187,17 @@ __device__ __forceinline__ void mul_pipelined(const Grp<G> &g, uint32_t *ws, con
   cp_async_wait<0>();
 }
 
+// sqrt may run CTAs of up to 8 warps (its lockstep warps then share the fetched code eight
+// at a time), with the same registers per thread as four-warp CTAs.
+template <int OP, int K>
+struct CtaBounds {
+  static constexpr int threads = OP == OP_SQRT ? 256 : 128;
+  static constexpr int min_blocks = OP == OP_SQRT ? (MinBlocks<OP, K>::v + 1) / 2 : MinBlocks<OP, K>::v;
+};
+
 template <int OP, int G, int K, int R>
-__global__ void __launch_bounds__(128, MinBlocks<OP, K>::v) k_elementwise(ElementwiseArgs args) {
+__global__ void __launch_bounds__(CtaBounds<OP, K>::threads, CtaBounds<OP, K>::min_blocks)
+    k_elementwise(ElementwiseArgs args) {
   extern __shared__ __align__(16) uint32_t smem[];
   Grp<G> g;
   const uint32_t gpc = blockDim.x / G, gi = threadIdx.x / G;
@@ -250,7 +259,9 @@ static cudaError_t launch_op(const ElementwiseArgs &args, cudaStream_t stream, i
   static int configured = 0, warps = 1, per_sm = 1;
   auto kern = k_elementwise<OP, G, K, R>;
   if (!configured) {
-    const int wmax = warp_bytes * 4 <= cta_max ? 4 : (warp_bytes * 2 <= cta_max ? 2 : 1);
+    const int wtop = CtaBounds<OP, K>::threads / 32;
+    int wmax = 1;
+    while (wmax * 2 <= wtop && warp_bytes * wmax * 2 <= cta_max) wmax *= 2;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(wmax * warp_bytes));
     if (e != cudaSuccess) return e;
