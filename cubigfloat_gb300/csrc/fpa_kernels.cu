@@ -252,10 +252,10 @@ static cudaError_t launch_op(const ElementwiseArgs &args, cudaStream_t stream, i
   constexpr size_t warp_bytes = (size_t)(32 / G) * Words<OP, G, K, R>::aligned() * sizeof(uint32_t);
   constexpr size_t cta_max = 227 * 1024;
   if constexpr (warp_bytes > cta_max) return cudaErrorInvalidConfiguration;
-  // CTA of 4, 2 or 1 warps: a smaller CTA is taken only when it keeps at least a quarter
-  // more warps resident on an SM (shared memory is granted per CTA, so where four warps'
-  // worth does not fit once more, a smaller CTA may still fit; measured, small CTAs are
-  // otherwise slightly slower).
+  // CTA of 4, 2 or 1 warps (sqrt: up to 8, CtaBounds): a smaller CTA is taken only when it
+  // keeps at least a quarter more warps resident on an SM (shared memory is granted per CTA,
+  // so where a larger CTA's worth does not fit once more, a smaller CTA may still fit;
+  // measured, small CTAs are otherwise slower).
   static int configured = 0, warps = 1, per_sm = 1;
   auto kern = k_elementwise<OP, G, K, R>;
   if (!configured) {
