@@ -57,6 +57,22 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def max_over_ranks(ms, device):
+    """The slowest replica's time: every rank contributes its own timed region, all get the
+    maximum (a collective on `device`; "cuda" under NCCL, "cpu" under gloo)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, ops_per_step, steps, max_ms):
+    """Whole-job throughput of `world` replicas that each ran `steps` steps of `ops_per_step`
+    operations, the slowest taking `max_ms`."""
+    return world * ops_per_step * steps / (max_ms / 1e3)
+
+
 class Clocks:
     """nvidia-smi samples during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -456,11 +472,9 @@ def run_gb300(args):
     per_op_ms = {op: float(np.mean([evs[s][op][0].elapsed_time(evs[s][op][1]) for s in range(args.steps)]))
                  for op in OPS}
     if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, "cuda")
     ops_per_step = len(OPS) * count
-    value = world * ops_per_step * args.steps / (total_ms / 1e3)
+    value = job_rate(world, ops_per_step, args.steps, total_ms)
     assert fpa.device_errors() == 0
 
     # e2e: the C-ABI with host buffers (pinned), copies inside the timed region
@@ -535,17 +549,15 @@ def run_gb300(args):
         torch.cuda.synchronize()
         ms = g0.elapsed_time(g1)
         if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+            ms = max_over_ranks(ms, "cuda")
         return ms
 
     e2e_sync_ms = timed_e2e(e2e_step, stream, stream)
     e2e_ms = timed_e2e(e2e_step_streams, s_in, s_out)
     h2d = sum((2 if op != "sqrt" else 1) * count * (4 + 4 * n) for op in OPS)
     d2h = len(OPS) * count * (4 + 4 * n)
-    e2e_val = world * ops_per_step * args.steps / (e2e_ms / 1e3)
-    e2e_sync_val = world * ops_per_step * args.steps / (e2e_sync_ms / 1e3)
+    e2e_val = job_rate(world, ops_per_step, args.steps, e2e_ms)
+    e2e_sync_val = job_rate(world, ops_per_step, args.steps, e2e_sync_ms)
 
     gpu_results = None
     if rank == 0 and not args.no_cpu:
