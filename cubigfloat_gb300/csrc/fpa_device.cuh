@@ -190,14 +190,19 @@ __device__ __forceinline__ uint32_t grp_sub(const Grp<G> &g, uint32_t *dst, X x,
   return bout;
 }
 
-// compare two numbers given as functors over [0, len): -1, 0, 1 (group-uniform)
+// compare two numbers given as functors over [0, len): -1, 0, 1 (group-uniform).
+// Each lane reduces 2*(index+1) + (x > y) at its highest differing limb, so the one
+// reduction yields both the top differing limb and the sign, and no lane reads the
+// operands after it (a caller may overwrite them right away).
 template <int G, class X, class Y>
 __device__ __forceinline__ int grp_cmp(const Grp<G> &g, X x, Y y, int len) {
-  uint32_t top = 0;                               // (index + 1) of my highest differing limb
-  for (int i = g.lane; i < len; i += G) if (x(i) != y(i)) top = (uint32_t)i + 1u;
-  top = g.rmax(top);
-  if (top == 0) return 0;
-  return x((int)top - 1) > y((int)top - 1) ? 1 : -1;
+  uint32_t key = 0;
+  for (int i = g.lane; i < len; i += G) {
+    const uint32_t xv = x(i), yv = y(i);
+    if (xv != yv) key = 2u * ((uint32_t)i + 1u) + (xv > yv ? 1u : 0u);
+  }
+  key = g.rmax(key);
+  return key == 0 ? 0 : ((key & 1u) ? 1 : -1);
 }
 
 template <int G, class X>

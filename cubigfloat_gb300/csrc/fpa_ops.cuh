@@ -889,7 +889,9 @@ __device__ void op_sqrt(const Grp<G> &g, uint32_t *ws, int n, int mode,
   grp_sub<G>(g, Rm, Shifted{Xh, n + 1, 32 * (n - 1)}, Ptr{V1, 2 * n + 3}, n + 2, 0u);
   // exact correction: 0 <= Rm <= 2S
   int guard = 0;
-  while ((Rm[n + 1] >> 31) != 0 && guard < 64) {       // Rm += 2S - 1, S -= 1
+  // the sign limb is read through a shuffle: every lane reads it before the shuffle, so the
+  // lane that owns it cannot overwrite it in the loop body while another lane still reads it
+  while ((g.bcast(Rm[n + 1], 0) >> 31) != 0 && guard < 64) {       // Rm += 2S - 1, S -= 1
     grp_add<G>(g, Rm, Ptr{Rm, n + 2}, ShlBits{S, n + 1, 1}, n + 2, 0u);
     grp_sub<G>(g, Rm, Ptr{Rm, n + 2}, Zero{}, n + 2, 1u);
     grp_sub<G>(g, S, Ptr{S, n + 1}, Zero{}, n + 1, 1u);
