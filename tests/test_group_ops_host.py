@@ -26,14 +26,24 @@ from test_gpu_rows import mul_cases
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, "cubigfloat_gb300", "csrc")
 
-# (G, K, R) of configurations 0, 2, 10, 12 and 15 -> sizes n <= G*K*R
+# (G, K, R) of the lane-group configurations the tuned table uses for mul, div and sqrt
+# (0, 1, 2, 3, 5, 6, 7, 10, 11, 12, 14) and configuration 15 -> sizes n <= G*K*R
 SHAPES = {
     (4, 2, 1): [1, 2, 3, 5, 8],
+    (8, 2, 1): [13, 16],
     (8, 4, 1): [9, 10, 17, 32],
+    (16, 4, 1): [64],
     (8, 4, 2): [33, 64],
+    (16, 8, 1): [128],
+    (8, 4, 4): [97, 128],
     (16, 4, 2): [100, 128],
     (4, 4, 8): [128],
+    (16, 8, 2): [256],
+    (32, 8, 1): [256],
+    (32, 16, 1): [512],
 }
+# operand-set sample per op at these sizes and above (first and last cases kept)
+SAMPLE_FROM, SAMPLE = 256, 48
 
 SHIMS = r"""
 #include <atomic>
@@ -239,12 +249,7 @@ int main() {
     memset(bt.re, 0xA5, (size_t)count * 4);
     memset(bt.r, 0xA5, (size_t)count * n * 4);
     switch (G * 10000 + K * 100 + R) {
-      case 40201: run_group<4, 2, 1>(&bt); break;
-      case 80401: run_group<8, 4, 1>(&bt); break;
-      case 80402: run_group<8, 4, 2>(&bt); break;
-      case 160402: run_group<16, 4, 2>(&bt); break;
-      case 40408: run_group<4, 4, 8>(&bt); break;
-      default: return 2;
+@CASES@      default: return 2;
     }
     printf("err %u\n", bt.err);
     for (int i = 0; i < count; i++) {
@@ -285,7 +290,9 @@ def host_source():
         body = body.replace(a, b)
     body = re.sub(r"#pragma unroll[^\n]*", "", body)
     assert "asm(" not in body and "asm volatile" not in body
-    return SHIMS + body + MAIN
+    cases = "".join(f"      case {G * 10000 + K * 100 + R}: run_group<{G}, {K}, {R}>(&bt); break;\n"
+                    for (G, K, R) in SHAPES)
+    return SHIMS + body + MAIN.replace("@CASES@", cases)
 
 
 @pytest.fixture(scope="module")
@@ -378,6 +385,8 @@ BIAS_W = W.BIAS
 def test_group_mul_div_sqrt_match_oracle(host_binary, shape, n):
     rng = np.random.default_rng(9100 + 7 * n + shape[0])
     cases = {2: mul_cases(rng, n), 3: div_cases(rng, n), 4: sqrt_cases(rng, n)}
+    if n >= SAMPLE_FROM:
+        cases = {op: _sample(c, SAMPLE) for op, c in cases.items()}
     batches = [(op, mode, cases[op]) for op in (2, 3, 4) for mode in range(5)]
     got = run_host(host_binary, shape, n, batches)
     for (op, mode, (ae, al, be, bl)), (err, ge, gl) in zip(batches, got):
@@ -393,6 +402,8 @@ def test_group_fma_matches_oracle(host_binary, shape, n):
     seeded = fma_cases(9300 + n + shape[0], n)
     special = special_cases(n)
     cases = tuple(np.concatenate([x, y]) for x, y in zip(seeded, special))
+    if n >= SAMPLE_FROM:
+        cases = _sample(cases, 2 * SAMPLE)
     batches = [(5, mode, cases) for mode in range(5)]
     got = run_host(host_binary, shape, n, batches)
     for (_, mode, c), (err, ge, gl) in zip(batches, got):
@@ -428,7 +439,7 @@ def tsan_binary(tmp_path_factory):
 
 
 @pytest.mark.parametrize("shape,n", [((4, 2, 1), 1), ((4, 2, 1), 8), ((8, 4, 1), 17), ((16, 4, 2), 128),
-                                     ((4, 4, 8), 128)])
+                                     ((4, 4, 8), 128), ((8, 4, 4), 128), ((32, 8, 1), 256)])
 def test_group_ops_have_no_lane_races(tsan_binary, shape, n, monkeypatch):
     """Lanes of a group share its workspace: every shared-memory word one lane writes and
     another reads (or writes) must be separated by a group sync or a collective.  The
@@ -438,7 +449,8 @@ def test_group_ops_have_no_lane_races(tsan_binary, shape, n, monkeypatch):
     fma = tuple(np.concatenate([x, y]) for x, y in zip(fma_cases(9600 + n, n), special_cases(n)))
     sets = {0: addsub_cases(rng, n), 2: mul_cases(rng, n), 3: div_cases(rng, n), 4: sqrt_cases(rng, n), 5: fma}
     sets[1] = sets[0]
-    batches = [(op, mode, _sample(sets[op], 60)) for op in (0, 1, 2, 3, 4, 5) for mode in (0, 3, 4)]
+    lim = 60 if n < SAMPLE_FROM else 24
+    batches = [(op, mode, _sample(sets[op], lim)) for op in (0, 1, 2, 3, 4, 5) for mode in (0, 3, 4)]
     monkeypatch.setenv("TSAN_OPTIONS", "halt_on_error=1 exitcode=66")
     got = run_host(tsan_binary, shape, n, batches)
     assert all(err == 0 for err, _, _ in got)
@@ -448,6 +460,8 @@ def test_group_ops_have_no_lane_races(tsan_binary, shape, n, monkeypatch):
 def test_group_addsub_matches_oracle(host_binary, shape, n):
     rng = np.random.default_rng(9700 + 7 * n + shape[0])
     cases = addsub_cases(rng, n)
+    if n >= SAMPLE_FROM:
+        cases = _sample(cases, 4 * SAMPLE)
     batches = [(op, mode, cases) for op in (0, 1) for mode in range(5)]
     got = run_host(host_binary, shape, n, batches)
     for (op, mode, c), (err, ge, gl) in zip(batches, got):
