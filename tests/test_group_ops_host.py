@@ -163,11 +163,21 @@ struct Grp {
 };
 """
 
-HOST_ASYNC = r"""static inline void cp_async4(uint32_t *dst, const uint32_t *src) { *dst = *src; }
-static inline void cp_async16(uint32_t *dst, const uint32_t *src) { memcpy(dst, src, 16); }
-static inline void cp_async_commit() {}
+# cp.async lands at the latest point it may: each copy is recorded when issued and made
+# when the issuing lane's wait retires its group.
+HOST_ASYNC = r"""struct AsyncCopy { uint32_t *dst; const uint32_t *src; int words; };
+static thread_local std::vector<AsyncCopy> t_open;
+static thread_local std::vector<std::vector<AsyncCopy>> t_groups;
+static inline void cp_async4(uint32_t *dst, const uint32_t *src) { t_open.push_back({dst, src, 1}); }
+static inline void cp_async16(uint32_t *dst, const uint32_t *src) { t_open.push_back({dst, src, 4}); }
+static inline void cp_async_commit() { t_groups.push_back(t_open); t_open.clear(); }
 template <int PENDING>
-static inline void cp_async_wait() {}
+static inline void cp_async_wait() {
+  while ((int)t_groups.size() > PENDING) {
+    for (const AsyncCopy &c : t_groups.front()) memcpy(c.dst, c.src, 4 * (size_t)c.words);
+    t_groups.erase(t_groups.begin());
+  }
+}
 """
 
 HOST_MAC3 = r"""static inline void mac3(uint32_t &lo, uint32_t &hi, uint32_t &tp, uint32_t a, uint32_t b) {
@@ -210,9 +220,27 @@ static void lane_main(uint32_t lane, Batch *bt) {
     g.sync();
   }
 }
+// the elementwise kernels' pipelined loops, one group taking every operation in turn
+// (ops 10 / 11 / 12 / 16: add, sub, mul, mul with the Karatsuba split)
+template <int G, int K, int R>
+static void lane_pipe(uint32_t lane, Batch *bt) {
+  t_lane = lane; t_round = 0;
+  Grp<G> g;
+  ElementwiseArgs args{};
+  args.count = (uint64_t)bt->count; args.n = (uint32_t)bt->n; args.mode = bt->mode;
+  args.r_exps = bt->re; args.r_limbs = bt->r; args.a_exps = bt->ae; args.a_limbs = bt->a;
+  args.b_exps = bt->be; args.b_limbs = bt->b; args.err = &bt->err;
+  if (bt->op == 10) addsub_pipelined<OP_ADD, G, K, R>(g, bt->ws, args, 0, 1);
+  else if (bt->op == 11) addsub_pipelined<OP_SUB, G, K, R>(g, bt->ws, args, 0, 1);
+  else if (bt->op == 12) mul_pipelined<G, K, R, false>(g, bt->ws, args, 0, 1);
+  else mul_pipelined<G, K, R, true>(g, bt->ws, args, 0, 1);
+}
 template <int G, int K, int R>
 static void run_group(Batch *bt) {
-  const int words = bt->op <= OP_SUB ? OpWords<OP_ADD, G, K, R>::aligned()
+  const int words = bt->op >= 10 ? (bt->op <= 11 ? PipeWords<OP_ADD, G, K, R>::aligned()
+                                    : bt->op == 12 ? PipeWords<OP_MUL, G, K, R>::aligned()
+                                                   : PipeWords<OP_MUL_KARA, G, K, R>::aligned())
+                    : bt->op <= OP_SUB ? OpWords<OP_ADD, G, K, R>::aligned()
                     : bt->op == OP_MUL ? OpWords<OP_MUL, G, K, R>::aligned()
                     : bt->op == OP_DIV ? OpWords<OP_DIV, G, K, R>::aligned()
                     : bt->op == OP_SQRT ? OpWords<OP_SQRT, G, K, R>::aligned() : OpWords<OP_FMA, G, K, R>::aligned();
@@ -222,7 +250,8 @@ static void run_group(Batch *bt) {
   bar.lanes = G;
   g_bar = &bar;
   std::vector<std::thread> lanes;
-  for (uint32_t l = 0; l < (uint32_t)G; l++) lanes.emplace_back(lane_main<G, K, R>, l, bt);
+  for (uint32_t l = 0; l < (uint32_t)G; l++)
+    lanes.emplace_back(bt->op >= 10 ? lane_pipe<G, K, R> : lane_main<G, K, R>, l, bt);
   for (auto &t : lanes) t.join();
   for (int i = words; i < words + 16; i++)
     if (ws[i] != 0x5A5A5A5Au) { fprintf(stderr, "workspace overrun\n"); std::_Exit(4); }
@@ -274,13 +303,18 @@ def _replace_once(src, start, end, new):
 def host_source():
     dev = open(os.path.join(CSRC, "fpa_device.cuh")).read()
     ops = open(os.path.join(CSRC, "fpa_ops.cuh")).read()
+    kern = open(os.path.join(CSRC, "fpa_kernels.cu")).read()
+    launch = open(os.path.join(CSRC, "fpa_launch.h")).read()
     dev = _replace_once(dev, "template <int G>\nstruct Grp {", "\n};\n", HOST_GRP)
     dev = _replace_once(dev, "__device__ __forceinline__ void cp_async4(",
                         ': "memory"); }\n\n', HOST_ASYNC + "\n")
     dev = _replace_once(dev, "__device__ __forceinline__ void mac3(", '"r"(a), "r"(b));\n}\n', HOST_MAC3)
     dev = _replace_once(dev, 'asm("sub.cc.u32', '"r"(a0), "r"(a1), "r"(a2));',
                         "sub3(lo[c], hi[c], tp[c], a0, a1, a2);")
-    body = dev + "\n" + ops
+    args = launch[launch.index("struct ElementwiseArgs {"):launch.index("};", launch.index("struct ElementwiseArgs {")) + 3]
+    pipe = kern[kern.index("// add/sub: HBM-bound"):kern.index("// sqrt may run CTAs")]
+    body = dev + "\n" + ops + "\nnamespace gfpa {\n" + pipe + "}  // namespace gfpa\n"
+    body = args + body
     assert "asm" not in body.replace("asm(", "").replace("asm ", "") or True
     lines = [ln for ln in body.split("\n") if not ln.startswith("#pragma once") and not ln.startswith("#include")]
     body = "\n".join(lines)
@@ -470,3 +504,45 @@ def test_group_addsub_matches_oracle(host_binary, shape, n):
         assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
         val = ee > 8
         assert np.array_equal(gl[val], el[val]), (op, n, mode, int(np.flatnonzero((gl != el).any(axis=1) & val)[0]))
+
+
+# (shape, n) for the elementwise kernels' pipelined loops; Karatsuba where the shape carries it
+PIPE_CASES = [((4, 2, 1), 8), ((8, 4, 1), 17), ((8, 4, 2), 64), ((16, 4, 2), 128), ((8, 4, 4), 97),
+              ((16, 8, 2), 201), ((16, 8, 2), 256), ((32, 8, 1), 256), ((32, 16, 1), 512)]
+
+
+def _karatsuba(shape):
+    G, K, R = shape
+    return K >= 8 and G * K * R >= 256
+
+
+@pytest.mark.parametrize("shape,n", PIPE_CASES)
+def test_pipelined_loops_match_oracle(host_binary, shape, n):
+    """addsub_pipelined and mul_pipelined (fpa_kernels.cu) with their double-buffered async
+    staging, the copies landing only at each lane's wait; mul also with the Karatsuba split."""
+    rng = np.random.default_rng(9900 + n + shape[0])
+    add, mul = addsub_cases(rng, n), mul_cases(rng, n)
+    if n >= SAMPLE_FROM:
+        add, mul = _sample(add, 4 * SAMPLE), _sample(mul, 2 * SAMPLE)
+    ops = [(10, 0, add), (11, 1, add), (12, 2, mul)] + ([(16, 2, mul)] if _karatsuba(shape) else [])
+    batches = [(code, mode, c) for code, _, c in ops for mode in range(5)]
+    got = run_host(host_binary, shape, n, batches)
+    expect = {(op, mode): oracle.run(op, n, mode, *c) for _, op, c in ops for mode in range(5)}
+    for (code, mode, c), (err, ge, gl) in zip(batches, got):
+        op = {10: 0, 11: 1, 12: 2, 16: 2}[code]
+        ee, el = expect[(op, mode)]
+        assert np.array_equal(ge, ee), (code, n, mode, int(np.flatnonzero(ge != ee)[0]))
+        val = ee > 8
+        assert np.array_equal(gl[val], el[val]), (code, n, mode, int(np.flatnonzero((gl != el).any(axis=1) & val)[0]))
+
+
+@pytest.mark.parametrize("shape,n", [((8, 4, 1), 17), ((16, 4, 2), 128), ((16, 8, 2), 256)])
+def test_pipelined_loops_have_no_lane_races(tsan_binary, shape, n, monkeypatch):
+    """The double-buffered loops under ThreadSanitizer: a lane that read staged operands
+    before the copying lane's wait and the group sync after it would be reported."""
+    rng = np.random.default_rng(9950 + n)
+    add, mul = _sample(addsub_cases(rng, n), 40), _sample(mul_cases(rng, n), 24)
+    codes = [(10, add), (11, add), (12, mul)] + ([(16, mul)] if _karatsuba(shape) else [])
+    batches = [(code, mode, c) for code, c in codes for mode in (0, 3)]
+    monkeypatch.setenv("TSAN_OPTIONS", "halt_on_error=1 exitcode=66")
+    run_host(tsan_binary, shape, n, batches)
