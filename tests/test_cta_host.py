@@ -1,0 +1,187 @@
+"""The elementwise kernel k_elementwise (cubigfloat_gb300/csrc/fpa_kernels.cu) for div, sqrt
+and fma, compiled for the host and run as whole CTAs: one host thread per GPU thread, each
+lane group with its own emulated collectives (as in test_group_ops_host.py), the CTA's
+shared memory one host buffer, and __syncthreads() a CTA barrier that also checks where it
+is called from.  The div/sqrt/fma loop makes every thread of a CTA run the same number of
+iterations and meet one CTA barrier per iteration, including the groups whose operation
+index is past the end.  On the GPU, bar.sync must be reached by all lanes of a warp at the
+same instruction; lanes that diverge onto two different barrier sites hang the CTA.  So the
+emulated barrier ends the program when two lanes of one warp arrive from different source
+lines, and a thread that skips a barrier makes the others time out.  Grids of 1 to 3 CTAs
+with 1, 2 or 4 warps per CTA, at operation counts that leave partial last iterations, are
+checked bit-exact against the oracle."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from fma_cases import fma_cases
+from test_group_ops_host import device_source, div_cases, sqrt_cases, _sample
+
+CTA_SHIMS = r"""
+#include <cstdint>
+struct HostDim3 { uint32_t x = 0, y = 0, z = 0; };
+static thread_local HostDim3 threadIdx, blockIdx;
+static HostDim3 blockDim, gridDim;
+static uint32_t *g_smem;
+"""
+
+CTA_BARRIER = r"""
+// CTA barrier: every thread records the source line it calls from; after all arrive, a
+// thread whose line differs from its warp's first lane's ends the program.
+static GroupBarrier g_cta_bar;
+static int g_cta_line[1024];
+static inline void cta_sync(int line) {
+  const uint32_t t = threadIdx.x;
+  g_cta_line[t] = line;
+  g_cta_bar.arrive_and_wait();
+  if (g_cta_line[t & ~31u] != line) {
+    fprintf(stderr, "warp %u: lanes at CTA barriers on lines %d and %d\n", t / 32, g_cta_line[t & ~31u], line);
+    std::_Exit(5);
+  }
+  g_cta_bar.arrive_and_wait();
+}
+#define __syncthreads() cta_sync(__LINE__)
+"""
+
+MAIN = r"""
+using namespace gfpa;
+static ElementwiseArgs g_args;
+template <int OP, int G, int K, int R>
+static void cta_thread(uint32_t tid, uint32_t block, GroupCtx *groups) {
+  threadIdx.x = tid; blockIdx.x = block;
+  t_lane = tid % G; t_ctx = &groups[tid / G]; t_round = 0;
+  k_elementwise<OP, G, K, R>(g_args);
+}
+template <int OP, int G, int K, int R>
+static void run_grid(int threads, int blocks) {
+  blockDim.x = threads; gridDim.x = blocks;
+  const int gpc = threads / G;
+  const size_t words = (size_t)gpc * PipeWords<OP, G, K, R>::aligned();
+  std::vector<uint32_t> smem(words + 64, 0x5A5A5A5Au);
+  g_smem = smem.data();
+  for (int b = 0; b < blocks; b++) {
+    std::vector<GroupCtx> groups(gpc);
+    for (auto &c : groups) c.bar.lanes = G;
+    g_cta_bar.lanes = threads;
+    std::vector<std::thread> ts;
+    for (int t = 0; t < threads; t++) ts.emplace_back(cta_thread<OP, G, K, R>, (uint32_t)t, (uint32_t)b, groups.data());
+    for (auto &t : ts) t.join();
+  }
+  for (size_t i = words; i < words + 64; i++)
+    if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
+}
+static uint32_t *alloc_words(size_t count) {
+  return static_cast<uint32_t *>(aligned_alloc(64, ((count * 4 + 63) / 64) * 64 + 64));
+}
+int main() {
+  int G, K, R, op, n, mode, count, warps, blocks;
+  while (scanf("%d %d %d %d %d %d %d %d %d", &G, &K, &R, &op, &n, &mode, &count, &warps, &blocks) == 9) {
+    uint32_t *ae = alloc_words(count), *be = alloc_words(count), *ce = alloc_words(count), *re = alloc_words(count);
+    uint32_t *a = alloc_words((size_t)count * n), *b = alloc_words((size_t)count * n);
+    uint32_t *c = alloc_words((size_t)count * n), *r = alloc_words((size_t)count * n);
+    for (int i = 0; i < count; i++) {
+      unsigned x;
+      if (scanf("%u", &x) != 1) return 1; ae[i] = x;
+      if (scanf("%u", &x) != 1) return 1; be[i] = x;
+      if (scanf("%u", &x) != 1) return 1; ce[i] = x;
+      for (int j = 0; j < n; j++) { if (scanf("%u", &x) != 1) return 1; a[(size_t)i * n + j] = x; }
+      for (int j = 0; j < n; j++) { if (scanf("%u", &x) != 1) return 1; b[(size_t)i * n + j] = x; }
+      for (int j = 0; j < n; j++) { if (scanf("%u", &x) != 1) return 1; c[(size_t)i * n + j] = x; }
+    }
+    memset(re, 0xA5, (size_t)count * 4);
+    memset(r, 0xA5, (size_t)count * n * 4);
+    uint32_t err = 0;
+    g_args = ElementwiseArgs{};
+    g_args.count = (uint64_t)count; g_args.n = (uint32_t)n; g_args.mode = mode;
+    g_args.r_exps = re; g_args.r_limbs = r; g_args.a_exps = ae; g_args.a_limbs = a;
+    g_args.b_exps = be; g_args.b_limbs = b; g_args.c_exps = ce; g_args.c_limbs = c; g_args.err = &err;
+    const int threads = 32 * warps, key = (G * 10000 + K * 100 + R) * 10 + op;
+    switch (key) {
+@CASES@      default: return 2;
+    }
+    printf("err %u\n", err);
+    for (int i = 0; i < count; i++) {
+      printf("%u", re[i]);
+      for (int j = 0; j < n; j++) printf(" %u", re[i] > CLS_SNAN ? r[(size_t)i * n + j] : 0u);
+      printf("\n");
+    }
+    free(ae); free(be); free(ce); free(re); free(a); free(b); free(c); free(r);
+  }
+  return 0;
+}
+"""
+
+SHAPES = [(4, 2, 1), (8, 4, 1), (16, 4, 2)]
+OPS = (3, 4, 5)                    # div, sqrt, fma
+
+
+def cta_source():
+    body = device_source("template <int OP, int G, int K, int R>\nusing Words",
+                         "template <int OP>\nstatic cudaError_t launch_op", CTA_SHIMS)
+    body = body.replace("extern __shared__ __align__(16) uint32_t smem[];", "uint32_t *smem = g_smem;")
+    head = "__global__ void __launch_bounds__(CtaBounds<OP, K>::threads, CtaBounds<OP, K>::min_blocks)"
+    assert body.count(head) == 1
+    body = body.replace(head, "void")
+    assert "__global__" not in body and "__shared__" not in body
+    # the CTA barrier goes after the group shims (it uses GroupBarrier), before the device code
+    mark = "template <int G>\nstruct Grp {"
+    body = body.replace(mark, "}  // namespace gfpa\n" + CTA_BARRIER + "namespace gfpa {\n" + mark, 1)
+    cases = "".join(f"      case {(G * 10000 + K * 100 + R) * 10 + op}: run_grid<{op}, {G}, {K}, {R}>(threads, blocks); "
+                    f"break;\n" for (G, K, R) in SHAPES for op in OPS)
+    return body + MAIN.replace("@CASES@", cases)
+
+
+def build(src_text, path, flags):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not found")
+    src, exe = path / "cta.cpp", path / "cta"
+    src.write_text(src_text)
+    r = subprocess.run([cxx] + flags + ["-std=c++20", "-fno-strict-aliasing", "-pthread", "-w", "-o", str(exe), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    return str(exe)
+
+
+@pytest.fixture(scope="module")
+def cta_binary(tmp_path_factory):
+    return build(cta_source(), tmp_path_factory.mktemp("cta"), ["-O2"])
+
+
+def run_cta(exe, shape, op, n, mode, case, warps, blocks):
+    G, K, R = shape
+    ae, al, be, bl = case[:4]
+    ce, cl = case[4:] if len(case) == 6 else (np.zeros_like(ae), np.zeros_like(al))
+    lines = [f"{G} {K} {R} {op} {n} {mode} {len(ae)} {warps} {blocks}"]
+    for i in range(len(ae)):
+        lines.append(f"{int(ae[i])} {int(be[i])} {int(ce[i])} " + " ".join(map(str, al[i])) + " "
+                     + " ".join(map(str, bl[i])) + " " + " ".join(map(str, cl[i])))
+    r = subprocess.run([exe], input="\n".join(lines) + "\n", capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
+    out = r.stdout.strip().split("\n")
+    rows = np.array([[int(x) for x in line.split()] for line in out[1:]], dtype=np.uint64)
+    return int(out[0].split()[1]), rows[:, 0].astype(np.uint32), rows[:, 1:].astype(np.uint32)
+
+
+# (shape, n, warps per CTA, CTAs, operations): counts leave the last iteration partial
+GRIDS = [((4, 2, 1), 5, 1, 2, 37), ((4, 2, 1), 8, 2, 3, 61), ((8, 4, 1), 17, 4, 1, 29), ((16, 4, 2), 128, 2, 2, 9)]
+
+
+@pytest.mark.parametrize("shape,n,warps,blocks,count", GRIDS)
+@pytest.mark.parametrize("op", OPS)
+def test_elementwise_kernel_lockstep_matches_oracle(cta_binary, shape, n, warps, blocks, count, op):
+    rng = np.random.default_rng(10100 + 10 * n + op)
+    case = {3: div_cases, 4: sqrt_cases}[op](rng, n) if op != 5 else fma_cases(10200 + n, n)
+    case = _sample(case, count)
+    for mode in (0, 3, 4):
+        err, ge, gl = run_cta(cta_binary, shape, op, n, mode, case, warps, blocks)
+        ee, el = oracle.run_fma(n, mode, *case) if op == 5 else (
+            oracle.run(op, n, mode, *case[:4]) if op == 3 else oracle.run(op, n, mode, *case[:2]))
+        assert err == 0
+        assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
+        val = ee > 8
+        assert np.array_equal(gl[val], el[val]), (op, n, mode)

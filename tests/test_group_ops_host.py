@@ -100,13 +100,16 @@ struct GroupBarrier {
     }
   }
 };
-static GroupBarrier *g_bar;
-static uint32_t g_slot[2][32];
+struct GroupCtx {                           // one lane group: its barrier and its two slot banks
+  GroupBarrier bar;
+  uint32_t slot[2][32];
+};
+static thread_local GroupCtx *t_ctx;
 static thread_local uint32_t t_lane, t_round;
 static inline const uint32_t *publish(uint32_t v) {
-  uint32_t *bank = g_slot[t_round++ & 1u];
+  uint32_t *bank = t_ctx->slot[t_round++ & 1u];
   bank[t_lane] = v;
-  g_bar->arrive_and_wait();
+  t_ctx->bar.arrive_and_wait();
   return bank;
 }
 static inline uint32_t __shfl_sync(uint32_t, uint32_t v, int src, int width) { return publish(v)[src & (width - 1)]; }
@@ -134,7 +137,7 @@ static inline void sub3(uint32_t &lo, uint32_t &hi, uint32_t &tp, uint32_t a0, u
 HOST_GRP = r"""template <int G>
 struct Grp {
   uint32_t lane = t_lane, base = 0, mask = G == 32 ? 0xFFFFFFFFu : ((1u << G) - 1u);
-  void sync() const { g_bar->arrive_and_wait(); }
+  void sync() const { t_ctx->bar.arrive_and_wait(); }
   uint32_t ballot(bool p) const {
     const uint32_t *b = publish(p ? 1u : 0u);
     uint32_t m = 0;
@@ -198,8 +201,8 @@ struct Batch {
   uint32_t err;
 };
 template <int G, int K, int R>
-static void lane_main(uint32_t lane, Batch *bt) {
-  t_lane = lane; t_round = 0;
+static void lane_main(uint32_t lane, Batch *bt, GroupCtx *ctx) {
+  t_lane = lane; t_round = 0; t_ctx = ctx;
   Grp<G> g;
   const int n = bt->n;
   for (int i = 0; i < bt->count; i++) {
@@ -223,8 +226,8 @@ static void lane_main(uint32_t lane, Batch *bt) {
 // the elementwise kernels' pipelined loops, one group taking every operation in turn
 // (ops 10 / 11 / 12 / 16: add, sub, mul, mul with the Karatsuba split)
 template <int G, int K, int R>
-static void lane_pipe(uint32_t lane, Batch *bt) {
-  t_lane = lane; t_round = 0;
+static void lane_pipe(uint32_t lane, Batch *bt, GroupCtx *ctx) {
+  t_lane = lane; t_round = 0; t_ctx = ctx;
   Grp<G> g;
   ElementwiseArgs args{};
   args.count = (uint64_t)bt->count; args.n = (uint32_t)bt->n; args.mode = bt->mode;
@@ -246,12 +249,11 @@ static void run_group(Batch *bt) {
                     : bt->op == OP_SQRT ? OpWords<OP_SQRT, G, K, R>::aligned() : OpWords<OP_FMA, G, K, R>::aligned();
   std::vector<uint32_t> ws((size_t)words + 16, 0x5A5A5A5Au);
   bt->ws = ws.data();
-  GroupBarrier bar;
-  bar.lanes = G;
-  g_bar = &bar;
+  GroupCtx ctx;
+  ctx.bar.lanes = G;
   std::vector<std::thread> lanes;
   for (uint32_t l = 0; l < (uint32_t)G; l++)
-    lanes.emplace_back(bt->op >= 10 ? lane_pipe<G, K, R> : lane_main<G, K, R>, l, bt);
+    lanes.emplace_back(bt->op >= 10 ? lane_pipe<G, K, R> : lane_main<G, K, R>, l, bt, &ctx);
   for (auto &t : lanes) t.join();
   for (int i = words; i < words + 16; i++)
     if (ws[i] != 0x5A5A5A5Au) { fprintf(stderr, "workspace overrun\n"); std::_Exit(4); }
@@ -300,6 +302,14 @@ def _replace_once(src, start, end, new):
     return src[:a] + new + src[b:]
 
 
+def _host_qualifiers(text):
+    for a, b in (("__device__ __forceinline__", "inline"), ("__device__ __noinline__", ""),
+                 ("__host__ __device__", ""), ("static __constant__", "static const"), ("__device__", ""),
+                 ("__restrict__", "__restrict")):
+        text = text.replace(a, b)
+    return re.sub(r"#pragma unroll[^\n]*", "", text)
+
+
 def host_source():
     dev = open(os.path.join(CSRC, "fpa_device.cuh")).read()
     ops = open(os.path.join(CSRC, "fpa_ops.cuh")).read()
@@ -318,15 +328,23 @@ def host_source():
     assert "asm" not in body.replace("asm(", "").replace("asm ", "") or True
     lines = [ln for ln in body.split("\n") if not ln.startswith("#pragma once") and not ln.startswith("#include")]
     body = "\n".join(lines)
-    for a, b in (("__device__ __forceinline__", "inline"), ("__device__ __noinline__", ""),
-                 ("__host__ __device__", ""), ("static __constant__", "static const"), ("__device__", ""),
-                 ("__restrict__", "__restrict")):
-        body = body.replace(a, b)
-    body = re.sub(r"#pragma unroll[^\n]*", "", body)
+    body = _host_qualifiers(body)
     assert "asm(" not in body and "asm volatile" not in body
     cases = "".join(f"      case {G * 10000 + K * 100 + R}: run_group<{G}, {K}, {R}>(&bt); break;\n"
                     for (G, K, R) in SHAPES)
     return SHIMS + body + MAIN.replace("@CASES@", cases)
+
+
+def device_source(kernel_start, kernel_end, extra_shims=""):
+    """SHIMS + fpa_device.cuh + fpa_ops.cuh + the part of fpa_kernels.cu between the two
+    markers, transformed for the host (no main)."""
+    src = host_source()
+    kern = open(os.path.join(CSRC, "fpa_kernels.cu")).read()
+    part = kern[kern.index(kernel_start):kern.index(kernel_end)]
+    a = src.index("namespace gfpa {\n// add/sub: HBM-bound")
+    b = src.index("}  // namespace gfpa\n", a) + len("}  // namespace gfpa\n")
+    part = _host_qualifiers(part)
+    return extra_shims + src[:a] + "namespace gfpa {\n" + part + "}  // namespace gfpa\n" + src[b:src.index(MAIN[:40])]
 
 
 @pytest.fixture(scope="module")
