@@ -19,7 +19,9 @@ import pytest
 
 import oracle
 from fma_cases import fma_cases
-from test_group_ops_host import device_source, div_cases, sqrt_cases, _sample
+from test_gpu_addsub import addsub_cases
+from test_gpu_rows import mul_cases
+from test_group_ops_host import CSRC, _host_qualifiers, device_source, div_cases, sqrt_cases, _sample
 
 CTA_SHIMS = r"""
 #include <cstdint>
@@ -74,6 +76,29 @@ static void run_grid(int threads, int blocks) {
   for (size_t i = words; i < words + 64; i++)
     if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
 }
+static BatchArgs g_bargs;
+template <int OP, int G, int K, int R>
+static void task_thread(uint32_t tid, GroupCtx *groups, uint32_t count) {
+  threadIdx.x = tid; blockIdx.x = 0;
+  t_lane = tid % G; t_ctx = &groups[tid / G]; t_round = 0;
+  run_task<OP, G, K, R>(g_bargs, 0, count, g_smem);
+}
+template <int OP, int G, int K, int R>
+static void run_batch_task(int threads, uint32_t count) {
+  blockDim.x = threads; gridDim.x = 1;
+  g_bargs.warp_words = (32 / G) * OpWords<OP, G, K, R>::aligned();
+  const size_t words = (size_t)(threads / 32) * g_bargs.warp_words;
+  std::vector<uint32_t> smem(words + 64, 0x5A5A5A5Au);
+  g_smem = smem.data();
+  std::vector<GroupCtx> groups(threads / G);
+  for (auto &c : groups) c.bar.lanes = G;
+  g_cta_bar.lanes = threads;
+  std::vector<std::thread> ts;
+  for (int t = 0; t < threads; t++) ts.emplace_back(task_thread<OP, G, K, R>, (uint32_t)t, groups.data(), count);
+  for (auto &t : ts) t.join();
+  for (size_t i = words; i < words + 64; i++)
+    if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
+}
 static uint32_t *alloc_words(size_t count) {
   return static_cast<uint32_t *>(aligned_alloc(64, ((count * 4 + 63) / 64) * 64 + 64));
 }
@@ -99,7 +124,23 @@ int main() {
     g_args.count = (uint64_t)count; g_args.n = (uint32_t)n; g_args.mode = mode;
     g_args.r_exps = re; g_args.r_limbs = r; g_args.a_exps = ae; g_args.a_limbs = a;
     g_args.b_exps = be; g_args.b_limbs = b; g_args.c_exps = ce; g_args.c_limbs = c; g_args.err = &err;
-    const int threads = 32 * warps, key = (G * 10000 + K * 100 + R) * 10 + op;
+    const int threads = 32 * warps, key = (G * 10000 + K * 100 + R) * 100 + op;
+    if (op >= 20) {                              // one batch task of `count` operations
+      std::vector<fpa_batch_desc> descs(count);
+      std::vector<uint32_t> order(count);
+      for (int i = 0; i < count; i++) {
+        descs[i] = fpa_batch_desc{(uint8_t)(op - 20), (uint8_t)mode, (uint16_t)n, 0u, (uint64_t)i * n,
+                                  (uint64_t)i * n, (uint64_t)i * n};
+        order[i] = (uint32_t)i;
+      }
+      g_bargs = BatchArgs{};
+      g_bargs.descs = descs.data(); g_bargs.order = order.data(); g_bargs.ntasks = 1;
+      g_bargs.r_exps = re; g_bargs.r_limbs = r; g_bargs.a_exps = ae; g_bargs.a_limbs = a;
+      g_bargs.b_exps = be; g_bargs.b_limbs = b; g_bargs.err = &err;
+      switch (key) {
+@BATCH_CASES@        default: return 2;
+      }
+    } else
     switch (key) {
 @CASES@      default: return 2;
     }
@@ -130,9 +171,22 @@ def cta_source():
     # the CTA barrier goes after the group shims (it uses GroupBarrier), before the device code
     mark = "template <int G>\nstruct Grp {"
     body = body.replace(mark, "}  // namespace gfpa\n" + CTA_BARRIER + "namespace gfpa {\n" + mark, 1)
-    cases = "".join(f"      case {(G * 10000 + K * 100 + R) * 10 + op}: run_grid<{op}, {G}, {K}, {R}>(threads, blocks); "
+    # the batched form's task body (fpa_batch_kernels.cu) and its argument structs
+    bk = open(os.path.join(CSRC, "fpa_batch_kernels.cu")).read()
+    task = bk[bk.index("template <int OP, int G, int K, int R>\n__device__ __noinline__ void run_task"):
+              bk.index("#define GFPA_TASK_OP")]
+    gh = open(os.path.join(CSRC, "..", "..", "include", "fpa_gb300.h")).read()
+    desc = gh[gh.index("typedef struct {\n  uint8_t op;"):gh.index("} fpa_batch_desc;") + len("} fpa_batch_desc;")]
+    bh = open(os.path.join(CSRC, "fpa_batch.h")).read()
+    structs = bh[bh.index("struct BatchTask {"):bh.index("// Tile width K of configuration")]
+    body = body.replace("template <int G>\nstruct Grp {", "}  // namespace gfpa\n" + desc + "\n" + structs
+                        + "namespace gfpa {\ntemplate <int G>\nstruct Grp {", 1)
+    body += "namespace gfpa {\n" + _host_qualifiers(task) + "}  // namespace gfpa\n"
+    cases = "".join(f"      case {(G * 10000 + K * 100 + R) * 100 + op}: run_grid<{op}, {G}, {K}, {R}>(threads, blocks); "
                     f"break;\n" for (G, K, R) in SHAPES for op in OPS)
-    return body + MAIN.replace("@CASES@", cases)
+    bcases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 20 + op}: run_batch_task<{op}, {G}, {K}, {R}>"
+                     f"(threads, (uint32_t)count); break;\n" for (G, K, R) in SHAPES for op in range(5))
+    return body + MAIN.replace("@CASES@", cases).replace("@BATCH_CASES@", bcases)
 
 
 def build(src_text, path, flags):
@@ -181,6 +235,23 @@ def test_elementwise_kernel_lockstep_matches_oracle(cta_binary, shape, n, warps,
         err, ge, gl = run_cta(cta_binary, shape, op, n, mode, case, warps, blocks)
         ee, el = oracle.run_fma(n, mode, *case) if op == 5 else (
             oracle.run(op, n, mode, *case[:4]) if op == 3 else oracle.run(op, n, mode, *case[:2]))
+        assert err == 0
+        assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
+        val = ee > 8
+        assert np.array_equal(gl[val], el[val]), (op, n, mode)
+
+
+@pytest.mark.parametrize("shape,n,warps,count", [((4, 2, 1), 5, 2, 37), ((8, 4, 1), 17, 4, 29), ((16, 4, 2), 128, 2, 9)])
+@pytest.mark.parametrize("op", range(5))
+def test_batch_task_lockstep_matches_oracle(cta_binary, shape, n, warps, count, op):
+    """run_task (fpa_batch_kernels.cu): one task of `count` operations on one CTA of several
+    warps.  div and sqrt run the lockstep loop with its single CTA barrier site."""
+    rng = np.random.default_rng(10300 + 10 * n + op)
+    make = {0: addsub_cases, 1: addsub_cases, 2: mul_cases, 3: div_cases, 4: sqrt_cases}[op]
+    case = _sample(make(rng, n), count)
+    for mode in (0, 3, 4):
+        err, ge, gl = run_cta(cta_binary, shape, 20 + op, n, mode, case, warps, 1)
+        ee, el = oracle.run(op, n, mode, *case[:4]) if op != 4 else oracle.run(op, n, mode, *case[:2])
         assert err == 0
         assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
         val = ee > 8
