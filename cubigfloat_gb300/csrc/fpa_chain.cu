@@ -61,7 +61,11 @@ __global__ void __launch_bounds__(128, 4) k_dot(ChainArgs A) {
       const uint64_t k = d * A.len + i, off = k * (uint64_t)n;
       op_mul<G, K, R>(g, ws, n, A.mode, A.x_exps[k], A.x_limbs + off, A.y_exps[k], A.y_limbs + off, tmp, tmp + 4);
       g.sync();
-      op_addsub<G, K, R>(g, ws, n, A.mode, 0, acc[0], acc + 4, tmp[0], tmp + 4, acc, acc + 4);
+      // every lane reads both exponent words before the sum may write acc[0] (a sum that is
+      // a copy of one operand writes it without meeting a collective first)
+      const uint32_t acc_e = acc[0], tmp_e = tmp[0];
+      g.sync();
+      op_addsub<G, K, R>(g, ws, n, A.mode, 0, acc_e, acc + 4, tmp_e, tmp + 4, acc, acc + 4);
       g.sync();
     }
     for (int i = g.lane; i < n; i += G) A.r_limbs[d * n + i] = acc[4 + i];

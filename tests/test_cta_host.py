@@ -18,8 +18,10 @@ import numpy as np
 import pytest
 
 import oracle
+from cubigfloat_gb300 import workloads as W
 from fma_cases import fma_cases
 from test_gpu_addsub import addsub_cases
+from test_gpu_chain import half, oracle_dot
 from test_gpu_rows import mul_cases
 from test_group_ops_host import CSRC, _host_qualifiers, device_source, div_cases, sqrt_cases, _sample
 
@@ -99,12 +101,38 @@ static void run_batch_task(int threads, uint32_t count) {
   for (size_t i = words; i < words + 64; i++)
     if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
 }
+static ChainArgs g_cargs;
+template <int KIND, int G, int K, int R>
+static void chain_thread(uint32_t tid, uint32_t block, GroupCtx *groups) {
+  threadIdx.x = tid; blockIdx.x = block;
+  t_lane = tid % G; t_ctx = &groups[tid / G]; t_round = 0;
+  if (KIND == 0) k_dot<G, K, R>(g_cargs);
+  else k_newton_sqrt<G, K, R>(g_cargs);
+}
+template <int KIND, int G, int K, int R>
+static void run_chain(int threads, int blocks) {
+  blockDim.x = threads; gridDim.x = blocks;
+  const int gpc = threads / G;
+  const size_t words = (size_t)gpc * (KIND == 0 ? ChainSpace<G, K, R>::dot() : ChainSpace<G, K, R>::newton());
+  std::vector<uint32_t> smem(words + 64, 0x5A5A5A5Au);
+  g_smem = smem.data();
+  for (int b = 0; b < blocks; b++) {
+    std::vector<GroupCtx> groups(gpc);
+    for (auto &c : groups) c.bar.lanes = G;
+    g_cta_bar.lanes = threads;
+    std::vector<std::thread> ts;
+    for (int t = 0; t < threads; t++) ts.emplace_back(chain_thread<KIND, G, K, R>, (uint32_t)t, (uint32_t)b, groups.data());
+    for (auto &t : ts) t.join();
+  }
+  for (size_t i = words; i < words + 64; i++)
+    if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
+}
 static uint32_t *alloc_words(size_t count) {
   return static_cast<uint32_t *>(aligned_alloc(64, ((count * 4 + 63) / 64) * 64 + 64));
 }
 int main() {
-  int G, K, R, op, n, mode, count, warps, blocks;
-  while (scanf("%d %d %d %d %d %d %d %d %d", &G, &K, &R, &op, &n, &mode, &count, &warps, &blocks) == 9) {
+  int G, K, R, op, n, mode, count, warps, blocks, len;
+  while (scanf("%d %d %d %d %d %d %d %d %d %d", &G, &K, &R, &op, &n, &mode, &count, &warps, &blocks, &len) == 10) {
     uint32_t *ae = alloc_words(count), *be = alloc_words(count), *ce = alloc_words(count), *re = alloc_words(count);
     uint32_t *a = alloc_words((size_t)count * n), *b = alloc_words((size_t)count * n);
     uint32_t *c = alloc_words((size_t)count * n), *r = alloc_words((size_t)count * n);
@@ -125,7 +153,18 @@ int main() {
     g_args.r_exps = re; g_args.r_limbs = r; g_args.a_exps = ae; g_args.a_limbs = a;
     g_args.b_exps = be; g_args.b_limbs = b; g_args.c_exps = ce; g_args.c_limbs = c; g_args.err = &err;
     const int threads = 32 * warps, key = (G * 10000 + K * 100 + R) * 100 + op;
-    if (op >= 20) {                              // one batch task of `count` operations
+    int results = count;
+    if (op >= 30) {                              // chains: dot (count / len dots) or Newton sqrt
+      g_cargs = ChainArgs{};
+      g_cargs.count = (uint64_t)(op == 30 ? count / len : count); g_cargs.n = (uint32_t)n;
+      g_cargs.len = (uint32_t)len; g_cargs.mode = mode;
+      g_cargs.r_exps = re; g_cargs.r_limbs = r; g_cargs.x_exps = ae; g_cargs.x_limbs = a;
+      g_cargs.y_exps = be; g_cargs.y_limbs = b; g_cargs.err = &err;
+      results = (int)g_cargs.count;
+      switch (key) {
+@CHAIN_CASES@        default: return 2;
+      }
+    } else if (op >= 20) {                              // one batch task of `count` operations
       std::vector<fpa_batch_desc> descs(count);
       std::vector<uint32_t> order(count);
       for (int i = 0; i < count; i++) {
@@ -145,7 +184,7 @@ int main() {
 @CASES@      default: return 2;
     }
     printf("err %u\n", err);
-    for (int i = 0; i < count; i++) {
+    for (int i = 0; i < results; i++) {
       printf("%u", re[i]);
       for (int j = 0; j < n; j++) printf(" %u", re[i] > CLS_SNAN ? r[(size_t)i * n + j] : 0u);
       printf("\n");
@@ -182,11 +221,20 @@ def cta_source():
     body = body.replace("template <int G>\nstruct Grp {", "}  // namespace gfpa\n" + desc + "\n" + structs
                         + "namespace gfpa {\ntemplate <int G>\nstruct Grp {", 1)
     body += "namespace gfpa {\n" + _host_qualifiers(task) + "}  // namespace gfpa\n"
+    # the fused chains (fpa_chain.cu)
+    ch = open(os.path.join(CSRC, "fpa_chain.cu")).read()
+    chain = _host_qualifiers(ch[ch.index("struct ChainArgs {"):ch.index("template <int G, int K, int R>\ncudaError_t launch_chain")])
+    assert chain.count("__global__ void __launch_bounds__(128, 4)") == 2
+    chain = chain.replace("__global__ void __launch_bounds__(128, 4)", "void")
+    chain = chain.replace("extern __shared__ __align__(16) uint32_t smem[];", "uint32_t *smem = g_smem;")
+    body += "namespace gfpa {\n" + chain + "}  // namespace gfpa\n"
     cases = "".join(f"      case {(G * 10000 + K * 100 + R) * 100 + op}: run_grid<{op}, {G}, {K}, {R}>(threads, blocks); "
                     f"break;\n" for (G, K, R) in SHAPES for op in OPS)
     bcases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 20 + op}: run_batch_task<{op}, {G}, {K}, {R}>"
                      f"(threads, (uint32_t)count); break;\n" for (G, K, R) in SHAPES for op in range(5))
-    return body + MAIN.replace("@CASES@", cases).replace("@BATCH_CASES@", bcases)
+    ccases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 30 + kind}: run_chain<{kind}, {G}, {K}, {R}>"
+                     f"(threads, blocks); break;\n" for (G, K, R) in SHAPES for kind in (0, 1))
+    return body + MAIN.replace("@CASES@", cases).replace("@BATCH_CASES@", bcases).replace("@CHAIN_CASES@", ccases)
 
 
 def build(src_text, path, flags):
@@ -206,11 +254,11 @@ def cta_binary(tmp_path_factory):
     return build(cta_source(), tmp_path_factory.mktemp("cta"), ["-O2"])
 
 
-def run_cta(exe, shape, op, n, mode, case, warps, blocks):
+def run_cta(exe, shape, op, n, mode, case, warps, blocks, length=0):
     G, K, R = shape
     ae, al, be, bl = case[:4]
     ce, cl = case[4:] if len(case) == 6 else (np.zeros_like(ae), np.zeros_like(al))
-    lines = [f"{G} {K} {R} {op} {n} {mode} {len(ae)} {warps} {blocks}"]
+    lines = [f"{G} {K} {R} {op} {n} {mode} {len(ae)} {warps} {blocks} {length}"]
     for i in range(len(ae)):
         lines.append(f"{int(ae[i])} {int(be[i])} {int(ce[i])} " + " ".join(map(str, al[i])) + " "
                      + " ".join(map(str, bl[i])) + " " + " ".join(map(str, cl[i])))
@@ -256,3 +304,70 @@ def test_batch_task_lockstep_matches_oracle(cta_binary, shape, n, warps, count, 
         assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
         val = ee > 8
         assert np.array_equal(gl[val], el[val]), (op, n, mode)
+
+
+@pytest.mark.parametrize("shape,n,warps,blocks,dots,length", [((4, 2, 1), 8, 2, 2, 37, 5), ((8, 4, 1), 17, 4, 1, 19, 4),
+                                                              ((16, 4, 2), 64, 2, 2, 9, 3)])
+def test_dot_chain_matches_stepwise_oracle(cta_binary, shape, n, warps, blocks, dots, length):
+    """k_dot (fpa_chain.cu): acc = RN(acc + RN(x*y)) over each dot's terms, against the
+    same steps in the oracle."""
+    rng = np.random.default_rng(10400 + n)
+    xe, xl = W.uniform(rng, dots * length, n, -30, 30)
+    ye, yl = W.uniform(rng, dots * length, n, -30, 30)
+    for mode in (1, 3):
+        err, ge, gl = run_cta(cta_binary, shape, 30, n, mode, (xe, xl, ye, yl), warps, blocks, length)
+        ee, el = oracle_dot(n, mode, xe, xl, ye, yl, dots, length)
+        assert err == 0 and np.array_equal(ge, ee) and np.array_equal(gl[ee > 8], el[ee > 8]), (n, mode)
+
+
+@pytest.mark.parametrize("shape,n,warps,blocks,count,iters", [((4, 2, 1), 5, 2, 2, 37, 4), ((8, 4, 1), 17, 4, 1, 29, 3),
+                                                              ((16, 4, 2), 128, 2, 2, 9, 2)])
+def test_newton_chain_lockstep_matches_stepwise_oracle(cta_binary, shape, n, warps, blocks, count, iters):
+    """k_newton_sqrt (fpa_chain.cu), whose rounds run in lockstep with one CTA barrier per
+    Newton step: y = RN(RN(y + RN(x/y)) * 0.5) against the same steps in the oracle."""
+    rng = np.random.default_rng(10500 + n)
+    xl = rng.integers(0, 1 << 32, size=(count, n), dtype=np.uint64).astype(np.uint32)
+    xl[:, -1] |= np.uint32(0x80000000)
+    xe = W.exp_word(np.ones(count, dtype=np.int64), 0)
+    yl = np.zeros((count, n), np.uint32)
+    yl[:, -1] = 0xC0000000
+    ye = W.exp_word(np.ones(count, dtype=np.int64), 0)
+    mode = 3
+    err, ge, gl = run_cta(cta_binary, shape, 31, n, mode, (xe, xl, ye, yl), warps, blocks, iters)
+    ee, el = ye.copy(), yl.copy()
+    for _ in range(iters):
+        te, tl = oracle.run(3, n, mode, xe, xl, ee, el)
+        se, sl = oracle.run(0, n, mode, ee, el, te, tl)
+        ee, el = half(se), sl
+    assert err == 0 and np.array_equal(ge, ee) and np.array_equal(gl, el)
+
+
+@pytest.fixture(scope="module")
+def cta_tsan_binary(tmp_path_factory):
+    try:
+        return build(cta_source(), tmp_path_factory.mktemp("cta_tsan"), ["-O1", "-g", "-fsanitize=thread"])
+    except AssertionError as e:
+        pytest.skip("ThreadSanitizer build failed: " + str(e)[-300:])
+
+
+@pytest.mark.parametrize("op", [3, 4, 5, 23, 24, 30, 31])
+def test_cta_kernels_have_no_lane_races(cta_tsan_binary, op, monkeypatch):
+    """The elementwise div/sqrt/fma loop, the batch div/sqrt task loop and both chains under
+    ThreadSanitizer on one shape (4x2x1, two warps, two CTAs where the kernel has a grid):
+    every shared word two lanes touch must be ordered by a group sync, a collective or the
+    CTA barrier."""
+    monkeypatch.setenv("TSAN_OPTIONS", "halt_on_error=1 exitcode=66")
+    rng = np.random.default_rng(10600 + op)
+    n, shape = 5, (4, 2, 1)
+    if op in (30, 31):
+        count, length = (45, 5) if op == 30 else (21, 3)
+        xe, xl = W.uniform(rng, count, n, -30, 30, signs=op == 30)
+        ye, yl = W.uniform(rng, count, n, -30, 30, signs=op == 30)
+        case, blocks = (xe, xl, ye, yl), 2
+    else:
+        base = op % 10
+        make = {3: div_cases, 4: sqrt_cases}.get(base)
+        case = _sample(make(rng, n) if make else fma_cases(10700, n), 40)
+        length, blocks = 0, 2 if op < 20 else 1
+    err, _, _ = run_cta(cta_tsan_binary, shape, op, n, 3, case, 2, blocks, length)
+    assert err == 0
