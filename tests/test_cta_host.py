@@ -49,6 +49,9 @@ static inline void cta_sync(int line) {
   g_cta_bar.arrive_and_wait();
 }
 #define __syncthreads() cta_sync(__LINE__)
+// __syncwarp(): the warp's barrier (the row kernel runs one operation per thread)
+static thread_local GroupBarrier *t_warp_bar;
+static inline void __syncwarp() { t_warp_bar->arrive_and_wait(); }
 """
 
 MAIN = r"""
@@ -127,6 +130,27 @@ static void run_chain(int threads, int blocks) {
   for (size_t i = words; i < words + 64; i++)
     if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
 }
+template <int OP, int N>
+static void rows_thread(uint32_t tid, uint32_t block, GroupBarrier *warp_bars) {
+  threadIdx.x = tid; blockIdx.x = block; t_warp_bar = &warp_bars[tid / 32];
+  k_rows<OP, N>(g_args);
+}
+template <int OP, int N>
+static void run_rows(int threads, int blocks) {
+  blockDim.x = threads; gridDim.x = blocks;
+  const size_t words = (size_t)(threads / 32) * RowSpace<N>::words;
+  std::vector<uint32_t> smem(words + 64, 0x5A5A5A5Au);
+  g_smem = smem.data();
+  for (int b = 0; b < blocks; b++) {
+    std::vector<GroupBarrier> bars(threads / 32);
+    for (auto &w : bars) w.lanes = 32;
+    std::vector<std::thread> ts;
+    for (int t = 0; t < threads; t++) ts.emplace_back(rows_thread<OP, N>, (uint32_t)t, (uint32_t)b, bars.data());
+    for (auto &t : ts) t.join();
+  }
+  for (size_t i = words; i < words + 64; i++)
+    if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
+}
 static uint32_t *alloc_words(size_t count) {
   return static_cast<uint32_t *>(aligned_alloc(64, ((count * 4 + 63) / 64) * 64 + 64));
 }
@@ -154,7 +178,20 @@ int main() {
     g_args.b_exps = be; g_args.b_limbs = b; g_args.c_exps = ce; g_args.c_limbs = c; g_args.err = &err;
     const int threads = 32 * warps, key = (G * 10000 + K * 100 + R) * 100 + op;
     int results = count;
-    if (op >= 30) {                              // chains: dot (count / len dots) or Newton sqrt
+    if (op >= 40) {                              // row kernels: op 40 + OP, n = 8, 16 or 32
+      switch ((op - 40) * 100 + n) {
+        case 8: run_rows<OP_ADD, 8>(threads, blocks); break;
+        case 16: run_rows<OP_ADD, 16>(threads, blocks); break;
+        case 32: run_rows<OP_ADD, 32>(threads, blocks); break;
+        case 108: run_rows<OP_SUB, 8>(threads, blocks); break;
+        case 116: run_rows<OP_SUB, 16>(threads, blocks); break;
+        case 132: run_rows<OP_SUB, 32>(threads, blocks); break;
+        case 208: run_rows<OP_MUL, 8>(threads, blocks); break;
+        case 216: run_rows<OP_MUL, 16>(threads, blocks); break;
+        case 232: run_rows<OP_MUL, 32>(threads, blocks); break;
+        default: return 2;
+      }
+    } else if (op >= 30) {                       // chains: dot (count / len dots) or Newton sqrt
       g_cargs = ChainArgs{};
       g_cargs.count = (uint64_t)(op == 30 ? count / len : count); g_cargs.n = (uint32_t)n;
       g_cargs.len = (uint32_t)len; g_cargs.mode = mode;
@@ -228,6 +265,14 @@ def cta_source():
     chain = chain.replace("__global__ void __launch_bounds__(128, 4)", "void")
     chain = chain.replace("extern __shared__ __align__(16) uint32_t smem[];", "uint32_t *smem = g_smem;")
     body += "namespace gfpa {\n" + chain + "}  // namespace gfpa\n"
+    # the one-thread row kernels (fpa_addsub_rows.cuh)
+    rw = open(os.path.join(CSRC, "fpa_addsub_rows.cuh")).read()
+    rows = _host_qualifiers(rw[rw.index("template <int N>\nstruct RowSpace"):
+                               rw.index("template <int OP, int N>\nstatic cudaError_t launch_rows")])
+    assert rows.count("__global__ void __launch_bounds__(128, 4)") == 1
+    rows = rows.replace("__global__ void __launch_bounds__(128, 4)", "void")
+    rows = rows.replace("extern __shared__ __align__(16) uint32_t smem[];", "uint32_t *smem = g_smem;")
+    body += "namespace gfpa {\n" + rows + "}  // namespace gfpa\n"
     cases = "".join(f"      case {(G * 10000 + K * 100 + R) * 100 + op}: run_grid<{op}, {G}, {K}, {R}>(threads, blocks); "
                     f"break;\n" for (G, K, R) in SHAPES for op in OPS)
     bcases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 20 + op}: run_batch_task<{op}, {G}, {K}, {R}>"
@@ -350,16 +395,20 @@ def cta_tsan_binary(tmp_path_factory):
         pytest.skip("ThreadSanitizer build failed: " + str(e)[-300:])
 
 
-@pytest.mark.parametrize("op", [3, 4, 5, 23, 24, 30, 31])
+@pytest.mark.parametrize("op", [3, 4, 5, 23, 24, 30, 31, 40, 42])
 def test_cta_kernels_have_no_lane_races(cta_tsan_binary, op, monkeypatch):
-    """The elementwise div/sqrt/fma loop, the batch div/sqrt task loop and both chains under
-    ThreadSanitizer on one shape (4x2x1, two warps, two CTAs where the kernel has a grid):
-    every shared word two lanes touch must be ordered by a group sync, a collective or the
-    CTA barrier."""
+    """Under ThreadSanitizer: the elementwise div/sqrt/fma loop, the batch div/sqrt task
+    loop, both chains (4x2x1 groups, 5 limbs) and the row kernel's add and mul (16 limbs),
+    on CTAs of two warps (two CTAs where the kernel has a grid).  Every shared word that two
+    threads touch must be ordered by a group sync, a collective, a warp sync or the CTA
+    barrier."""
     monkeypatch.setenv("TSAN_OPTIONS", "halt_on_error=1 exitcode=66")
     rng = np.random.default_rng(10600 + op)
     n, shape = 5, (4, 2, 1)
-    if op in (30, 31):
+    if op >= 40:
+        n = 16
+        case, length, blocks = _sample((addsub_cases if op == 40 else mul_cases)(rng, n), 70), 0, 2
+    elif op in (30, 31):
         count, length = (45, 5) if op == 30 else (21, 3)
         xe, xl = W.uniform(rng, count, n, -30, 30, signs=op == 30)
         ye, yl = W.uniform(rng, count, n, -30, 30, signs=op == 30)
@@ -371,3 +420,20 @@ def test_cta_kernels_have_no_lane_races(cta_tsan_binary, op, monkeypatch):
         length, blocks = 0, 2 if op < 20 else 1
     err, _, _ = run_cta(cta_tsan_binary, shape, op, n, 3, case, 2, blocks, length)
     assert err == 0
+
+
+@pytest.mark.parametrize("n", [8, 16, 32])
+@pytest.mark.parametrize("op", [0, 1, 2])
+def test_row_kernel_matches_oracle(cta_binary, op, n):
+    """k_rows (fpa_addsub_rows.cuh) as whole emulated CTAs of four warps: each warp stages 32
+    operations' rows cooperatively (async copies landing at each thread's wait), syncs,
+    computes one operation per thread and copies the results out cooperatively.  The
+    operation counts leave a partial last chunk of 32."""
+    rng = np.random.default_rng(10800 + 10 * n + op)
+    case = (addsub_cases if op < 2 else mul_cases)(rng, n)
+    case = _sample(case, 300)
+    for mode in (0, 3):
+        err, ge, gl = run_cta(cta_binary, (4, 2, 1), 40 + op, n, mode, case, 4, 2)
+        ee, el = oracle.run(op, n, mode, *case[:4])
+        assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
+        assert np.array_equal(gl[ee > 8], el[ee > 8]), (op, n, mode)
