@@ -130,6 +130,23 @@ static void run_chain(int threads, int blocks) {
   for (size_t i = words; i < words + 64; i++)
     if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
 }
+template <int OP, int G, int K>
+static void regk_thread(uint32_t tid, uint32_t block, GroupCtx *groups) {
+  threadIdx.x = tid; blockIdx.x = block;
+  t_lane = tid % G; t_ctx = &groups[tid / G]; t_round = 0;
+  k_addsub_regk<OP, G, K>(g_args);
+}
+template <int OP, int G, int K>
+static void run_regk(int threads, int blocks) {
+  blockDim.x = threads; gridDim.x = blocks;
+  for (int b = 0; b < blocks; b++) {
+    std::vector<GroupCtx> groups(threads / G);
+    for (auto &c : groups) c.bar.lanes = G;
+    std::vector<std::thread> ts;
+    for (int t = 0; t < threads; t++) ts.emplace_back(regk_thread<OP, G, K>, (uint32_t)t, (uint32_t)b, groups.data());
+    for (auto &t : ts) t.join();
+  }
+}
 template <int OP, int N>
 static void rows_thread(uint32_t tid, uint32_t block, GroupBarrier *warp_bars) {
   threadIdx.x = tid; blockIdx.x = block; t_warp_bar = &warp_bars[tid / 32];
@@ -178,7 +195,11 @@ int main() {
     g_args.b_exps = be; g_args.b_limbs = b; g_args.c_exps = ce; g_args.c_limbs = c; g_args.err = &err;
     const int threads = 32 * warps, key = (G * 10000 + K * 100 + R) * 100 + op;
     int results = count;
-    if (op >= 40) {                              // row kernels: op 40 + OP, n = 8, 16 or 32
+    if (op >= 50) {                              // register add/sub kernel: op 50 + OP
+      switch (key - (op - 50)) {
+@REGK_CASES@        default: return 2;
+      }
+    } else if (op >= 40) {                       // row kernels: op 40 + OP, n = 8, 16 or 32
       switch ((op - 40) * 100 + n) {
         case 8: run_rows<OP_ADD, 8>(threads, blocks); break;
         case 16: run_rows<OP_ADD, 16>(threads, blocks); break;
@@ -273,13 +294,23 @@ def cta_source():
     rows = rows.replace("__global__ void __launch_bounds__(128, 4)", "void")
     rows = rows.replace("extern __shared__ __align__(16) uint32_t smem[];", "uint32_t *smem = g_smem;")
     body += "namespace gfpa {\n" + rows + "}  // namespace gfpa\n"
+    # the register add/sub kernel (fpa_addsub_regs.cuh)
+    rg = open(os.path.join(CSRC, "fpa_addsub_regs.cuh")).read()
+    regk = _host_qualifiers(rg[rg.index("template <int K>\nstruct Log2"):
+                               rg.index("template <int OP, int G, int K>\nstatic cudaError_t launch_addsub_regk")])
+    head = "__global__ void __launch_bounds__(128, (K <= 4) ? 8 : (K <= 8 ? 4 : 2))"
+    assert regk.count(head) == 1
+    body += "namespace gfpa {\n" + regk.replace(head, "void") + "}  // namespace gfpa\n"
     cases = "".join(f"      case {(G * 10000 + K * 100 + R) * 100 + op}: run_grid<{op}, {G}, {K}, {R}>(threads, blocks); "
                     f"break;\n" for (G, K, R) in SHAPES for op in OPS)
     bcases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 20 + op}: run_batch_task<{op}, {G}, {K}, {R}>"
                      f"(threads, (uint32_t)count); break;\n" for (G, K, R) in SHAPES for op in range(5))
     ccases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 30 + kind}: run_chain<{kind}, {G}, {K}, {R}>"
                      f"(threads, blocks); break;\n" for (G, K, R) in SHAPES for kind in (0, 1))
-    return body + MAIN.replace("@CASES@", cases).replace("@BATCH_CASES@", bcases).replace("@CHAIN_CASES@", ccases)
+    rcases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 50}: "
+                     f"if (op == 50) run_regk<OP_ADD, {G}, {K}>(threads, blocks); "
+                     f"else run_regk<OP_SUB, {G}, {K}>(threads, blocks); break;\n" for (G, K, R) in SHAPES)
+    return body + MAIN.replace("@REGK_CASES@", rcases).replace("@CASES@", cases).replace("@BATCH_CASES@", bcases).replace("@CHAIN_CASES@", ccases)
 
 
 def build(src_text, path, flags):
@@ -434,6 +465,21 @@ def test_row_kernel_matches_oracle(cta_binary, op, n):
     case = _sample(case, 300)
     for mode in (0, 3):
         err, ge, gl = run_cta(cta_binary, (4, 2, 1), 40 + op, n, mode, case, 4, 2)
+        ee, el = oracle.run(op, n, mode, *case[:4])
+        assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
+        assert np.array_equal(gl[ee > 8], el[ee > 8]), (op, n, mode)
+
+
+@pytest.mark.parametrize("shape,n", [((4, 2, 1), 8), ((4, 2, 1), 5), ((8, 4, 1), 32), ((8, 4, 1), 19), ((16, 4, 2), 64)])
+@pytest.mark.parametrize("op", [0, 1])
+def test_register_addsub_kernel_matches_oracle(cta_binary, shape, n, op):
+    """k_addsub_regk (fpa_addsub_regs.cuh) as emulated CTAs of four warps on a grid of two:
+    the grid-stride loop that loads the next operation's operands into registers while the
+    group computes the current one, at counts that leave groups without a last operation."""
+    rng = np.random.default_rng(10900 + n + op)
+    case = _sample(addsub_cases(rng, n), 150)
+    for mode in (0, 3):
+        err, ge, gl = run_cta(cta_binary, shape, 50 + op, n, mode, case, 4, 2)
         ee, el = oracle.run(op, n, mode, *case[:4])
         assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
         assert np.array_equal(gl[ee > 8], el[ee > 8]), (op, n, mode)
