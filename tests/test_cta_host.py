@@ -23,7 +23,7 @@ from fma_cases import fma_cases
 from test_gpu_addsub import addsub_cases
 from test_gpu_chain import half, oracle_dot
 from test_gpu_rows import mul_cases
-from test_group_ops_host import CSRC, _host_qualifiers, device_source, div_cases, sqrt_cases, _sample
+from test_group_ops_host import CSRC, _host_qualifiers, device_source, div_cases, sqrt_cases, _sample, tsan_starts
 
 CTA_SHIMS = r"""
 #include <cstdint>
@@ -421,9 +421,11 @@ def test_newton_chain_lockstep_matches_stepwise_oracle(cta_binary, shape, n, war
 @pytest.fixture(scope="module")
 def cta_tsan_binary(tmp_path_factory):
     try:
-        return build(cta_source(), tmp_path_factory.mktemp("cta_tsan"), ["-O1", "-g", "-fsanitize=thread"])
+        exe = build(cta_source(), tmp_path_factory.mktemp("cta_tsan"), ["-O1", "-g", "-fsanitize=thread"])
     except AssertionError as e:
         pytest.skip("ThreadSanitizer build failed: " + str(e)[-300:])
+    tsan_starts(exe)
+    return exe
 
 
 @pytest.mark.parametrize("op", [3, 4, 5, 23, 24, 30, 31, 40, 42])

@@ -487,7 +487,16 @@ def tsan_binary(tmp_path_factory):
                         "-fsanitize=thread", "-o", str(exe), str(src)], capture_output=True, text=True)
     if r.returncode != 0:
         pytest.skip("ThreadSanitizer is not available: " + r.stderr[-300:])
+    tsan_starts(str(exe))
     return str(exe)
+
+
+def tsan_starts(exe):
+    """Skip when a ThreadSanitizer build cannot start on this host (it refuses some memory
+    layouts); an empty input makes the program exit at once."""
+    r = subprocess.run([exe], input="", capture_output=True, text=True, timeout=120)
+    if r.returncode != 0 and "ThreadSanitizer" in r.stderr:
+        pytest.skip("ThreadSanitizer cannot run here: " + r.stderr.strip()[-300:])
 
 
 @pytest.mark.parametrize("shape,n", [((4, 2, 1), 1), ((4, 2, 1), 8), ((8, 4, 1), 17), ((16, 4, 2), 128),
