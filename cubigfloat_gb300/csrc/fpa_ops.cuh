@@ -155,145 +155,6 @@ __device__ void op_addsub(const Grp<G> &g, uint32_t *ws, int n, int mode, int is
 }
 
 // ---------------------------------------------------------------------------------------
-// add/sub held in registers, for n <= G: lane l holds limb l of each operand, the aligned
-// sum is formed with shuffles and carry lookahead, and rounded with ballots (no shared
-// memory).  Same semantics and result as op_addsub (X = BIG*2^64 +- floor(SMALL*2^(64-d)),
-// lost bits as sticky / borrow, one rounding).
-template <int G>
-__device__ __forceinline__ uint32_t lane_shfl(const Grp<G> &g, uint32_t v, int src, bool ok) {
-  const uint32_t r = __shfl_sync(g.mask, v, ok ? src : 0, G);
-  return ok ? r : 0u;
-}
-
-template <int G>
-__device__ void op_addsub_reg(const Grp<G> &g, int n, int mode, int is_sub, uint32_t a_exp, const uint32_t *a,
-                              uint32_t b_exp, const uint32_t *b, uint32_t *r_exp, uint32_t *r) {
-  const int l = (int)g.lane;
-  const uint32_t act = c_action[is_sub][classify(a_exp) * 9 + classify(b_exp)];
-  const uint32_t av = l < n ? a[l] : 0u, bv = l < n ? b[l] : 0u;
-  if (act == ACT_COPY_A || act == ACT_COPY_B || act == ACT_NEG_B) {
-    const uint32_t e = act == ACT_COPY_A ? a_exp : (act == ACT_COPY_B ? b_exp : b_exp ^ 1u);
-    if (l < n) r[l] = act == ACT_COPY_A ? av : bv;
-    if (l == 0) *r_exp = e;
-    return;
-  }
-  if (act != ACT_ADD && act != ACT_SUB) { if (l == 0) *r_exp = act; return; }
-  const uint32_t sa = a_exp & 1u, sb = (b_exp & 1u) ^ (uint32_t)is_sub;
-  const long long ea = (long long)(a_exp >> 1) - BIAS, eb = (long long)(b_exp >> 1) - BIAS;
-  const bool eff_sub = sa != sb;
-  bool a_big;
-  if (ea != eb) a_big = ea > eb;
-  else {
-    const uint32_t dm = g.ballot(av != bv);
-    if (dm == 0 && eff_sub) { if (l == 0) *r_exp = CLS_ZERO; return; }   // exact cancellation
-    const int t = dm ? 31 - __clz((int)dm) : 0;
-    const uint32_t at = g.bcast(av, t), bt = g.bcast(bv, t);
-    a_big = dm == 0 || at > bt;
-  }
-  const uint32_t big = a_big ? av : bv, sml = a_big ? bv : av;
-  const uint32_t sign = a_big ? sa : sb;
-  const long long ebig = a_big ? ea : eb, esml = a_big ? eb : ea;
-  const long long cap = 32LL * n + 64;
-  const int d = (int)((ebig - esml) > cap ? cap : (ebig - esml));
-  const int dw = d >> 5, db = d & 31;
-  // limb i of floor(SMALL * 2^(64-d)) = SMALL bits from 32(i-2+dw) + db
-  auto slimb = [&](int q) -> uint32_t {          // SMALL limb q shifted right by db, with q+1 above
-    const uint32_t lo = lane_shfl<G>(g, sml, q, q >= 0 && q < n);
-    const uint32_t hi = lane_shfl<G>(g, sml, q + 1, q + 1 >= 0 && q + 1 < n);
-    return db ? ((lo >> db) | (hi << (32 - db))) : lo;
-  };
-  const uint32_t s_main = slimb(l + dw);                       // X limb l+2
-  const uint32_t s0 = slimb(dw - 2), s1 = slimb(dw - 1);       // guard limbs X[0], X[1]
-  // bits of SMALL below X[0] (d > 64): sticky, and one more unit off an effective subtraction
-  uint32_t lostv = 0;
-  if (d > 64) {
-    const int cut = d - 64, full = cut >> 5;
-    if (l < full && l < n) lostv = sml;
-    if (l == full && (cut & 31) && full < n) lostv = sml & ((1u << (cut & 31)) - 1u);
-  }
-  const uint32_t lost = g.ballot(lostv != 0) != 0;
-  // guard limbs, then the main limbs with carry lookahead; lane n (if any) takes the top limb
-  uint32_t x0, x1, cin;
-  if (!eff_sub) { x0 = s0; x1 = s1; cin = 0; }
-  else {
-    const uint64_t t0 = (uint64_t)0 - s0 - lost;
-    x0 = (uint32_t)t0;
-    const uint32_t b0 = (s0 != 0 || lost) ? 1u : 0u;
-    const uint64_t t1 = (uint64_t)0 - s1 - b0;
-    x1 = (uint32_t)t1;
-    cin = (s1 != 0 || b0) ? 1u : 0u;                          // borrow into the main limbs
-  }
-  uint32_t v, gen, prop;
-  if (!eff_sub) {
-    const uint64_t t = (uint64_t)big + s_main;
-    v = (uint32_t)t; gen = (uint32_t)(t >> 32); prop = v == 0xFFFFFFFFu && !gen;
-  } else {
-    v = big - s_main; gen = big < s_main; prop = v == 0u && !gen;
-  }
-  uint32_t cout;
-  const uint64_t cv = lookahead<G>(g.ballot(gen != 0), g.ballot(prop != 0), cin, cout);
-  const uint32_t c_in = (uint32_t)(cv >> l) & 1u;
-  v = eff_sub ? v - c_in : v + c_in;
-  const uint32_t xtop = eff_sub ? 0u : cout;                   // X limb G+2 (only when n == G)
-  // bit length of X (limbs: x0, x1, lanes 0..G-1 as limbs 2..G+1, xtop as limb G+2)
-  const uint32_t nz = g.ballot(v != 0);
-  int L;
-  if (xtop) L = 32 * (G + 2) + 32 - (int)clz32(xtop);
-  else if (nz) { const int t = 31 - __clz((int)nz); L = 32 * (t + 2) + 32 - (int)clz32(g.bcast(v, t)); }
-  else if (x1) L = 32 + 32 - (int)clz32(x1);
-  else if (x0) L = 32 - (int)clz32(x0);
-  else { if (l == 0) *r_exp = CLS_ZERO; return; }
-  // X limb k for any k (uniform k across the group is not required)
-  auto xlimb = [&](int k) -> uint32_t {
-    const uint32_t m = lane_shfl<G>(g, v, k - 2, k - 2 >= 0 && k - 2 < G);
-    return k == 0 ? x0 : (k == 1 ? x1 : (k == G + 2 ? xtop : (k < 0 || k > G + 2 ? 0u : m)));
-  };
-  const int lo = L - 32 * n;                                   // bit of X at the mantissa's bit 0
-  const int lw = lo >> 5, lb = lo & 31;                         // floor division
-  uint32_t mant;
-  {
-    const uint32_t p = xlimb(l + lw), q = xlimb(l + lw + 1);
-    mant = lb ? ((p >> lb) | (q << (32 - lb))) : p;
-    if (l >= n) mant = 0;
-  }
-  uint32_t rbit = 0, st = 0;
-  if (lo >= 1) {
-    const int rp = lo - 1;
-    rbit = (xlimb(rp >> 5) >> (rp & 31)) & 1u;                  // the same limb in every lane
-    // sticky: limbs of X fully below the round limb, and the low bits of the round limb
-    const int full = rp >> 5;
-    const uint32_t xf = xlimb(full);                            // every lane: shuffles are collective
-    uint32_t part = 0;
-    if (l + 2 < full) part |= v;                                // main limbs below
-    if (l == 0) {
-      if (full > 0) part |= x0;
-      if (full > 1) part |= x1;
-      if (rp & 31) part |= xf & ((1u << (rp & 31)) - 1u);
-    }
-    st = g.ror(part);
-  }
-  st |= lost;
-  const uint32_t lsb = g.bcast(mant, 0) & 1u;
-  int ovf = 0;
-  if (round_up(mode, sign, lsb, rbit, st != 0)) {
-    const uint32_t ones = g.ballot(l >= n || mant == 0xFFFFFFFFu);
-    const uint32_t need = (G == 32) ? 0xFFFFFFFFu : ((1u << G) - 1u);
-    // carry into lane l: all lanes below are all ones
-    const uint32_t below = (l == 0) ? 0u : ((1u << l) - 1u);
-    if ((ones & below) == below && l < n) mant += 1u;
-    if ((ones & need) == need) {                               // 0.11..1 + ulp = 1.0
-      ovf = 1;
-      mant = (l == n - 1) ? 0x80000000u : 0u;
-    }
-  }
-  const long long e = ebig - 32LL * n - 64 + L + ovf;
-  if (!eff_sub && (long long)BIAS + e > 0x7FFFFFFFLL) { if (l == 0) *r_exp = CLS_POS_INF - sign; return; }
-  if (eff_sub && (long long)BIAS + e < 5) { if (l == 0) *r_exp = CLS_POS_TINY - sign; return; }
-  if (l < n) r[l] = mant;
-  if (l == 0) *r_exp = exp_word(e, sign);
-}
-
-// ---------------------------------------------------------------------------------------
 // Karatsuba split of a staged square product (x in s.sa, y in s.sb + K, n limbs each):
 //   P[0..2n) = z0 + z1 2^(32h) + z2 2^(64h),  h = ceil(n/2),
 //   z0 = x0 y0,  z2 = x1 y1,  z1 = (x0 + x1)(y0 + y1) - z0 - z2.
