@@ -31,6 +31,7 @@ struct HostDim3 { uint32_t x = 0, y = 0, z = 0; };
 static thread_local HostDim3 threadIdx, blockIdx;
 static HostDim3 blockDim, gridDim;
 static uint32_t *g_smem;
+static inline uint32_t atomicAdd(uint32_t *p, uint32_t v) { return __atomic_fetch_add(p, v, __ATOMIC_RELAXED); }
 """
 
 CTA_BARRIER = r"""
@@ -168,6 +169,67 @@ static void run_rows(int threads, int blocks) {
   for (size_t i = words; i < words + 64; i++)
     if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
 }
+template <int OP, int G, int K, int R>
+constexpr uint32_t warp_words_of() { return (32 / G) * OpWords<OP, G, K, R>::aligned(); }
+// shared-memory words per warp of a class kernel: the largest task body it may run
+static uint32_t class_warp_words(int cls) {
+  const uint32_t w[2][3] = {
+      {std::max(warp_words_of<OP_ADD, 4, 2, 1>(), warp_words_of<OP_MUL, 4, 2, 1>()),
+       std::max(warp_words_of<OP_ADD, 8, 4, 1>(), warp_words_of<OP_MUL, 8, 4, 1>()),
+       std::max(warp_words_of<OP_ADD, 16, 4, 2>(), warp_words_of<OP_MUL, 16, 4, 2>())},
+      {std::max(warp_words_of<OP_DIV, 4, 2, 1>(), warp_words_of<OP_SQRT, 4, 2, 1>()),
+       std::max(warp_words_of<OP_DIV, 8, 4, 1>(), warp_words_of<OP_SQRT, 8, 4, 1>()),
+       std::max(warp_words_of<OP_DIV, 16, 4, 2>(), warp_words_of<OP_SQRT, 16, 4, 2>())}};
+  return std::max(std::max(w[cls][0], w[cls][1]), w[cls][2]);
+}
+template <int CLS>
+static void dispatch_thread(uint32_t tid, uint32_t block, GroupCtx *groups, int G) {
+  threadIdx.x = tid; blockIdx.x = block;
+  t_lane = tid % G; t_ctx = &groups[tid / G]; t_round = 0;
+  k_batch<CLS>(g_bargs);
+}
+// a mixed batch: operation i is ce[i] (0..4), all on configuration cfg; tasks of at most 7
+// operations in descriptor order, class 0 (add/sub/mul) and class 1 (div/sqrt) kernels
+static int run_dispatch(int cfg, int G, int n, int mode, int count, int blocks, const uint32_t *ops,
+                        std::vector<fpa_batch_desc> &descs) {
+  std::vector<uint32_t> order(count);
+  std::vector<BatchTask> tasks[2];
+  for (int i = 0; i < count; i++) {
+    descs[i] = fpa_batch_desc{(uint8_t)ops[i], (uint8_t)mode, (uint16_t)n, 0u, (uint64_t)i * n, (uint64_t)i * n,
+                              (uint64_t)i * n};
+    order[i] = (uint32_t)i;
+  }
+  for (int i = 0; i < count;) {
+    int j = i;
+    while (j < count && j - i < 7 && ops[j] == ops[i]) j++;
+    tasks[ops[i] >= 3].push_back(BatchTask{(uint16_t)(cfg * 5 + ops[i]), 0, (uint32_t)i, (uint32_t)(j - i)});
+    i = j;
+  }
+  g_bargs.descs = descs.data(); g_bargs.order = order.data();
+  for (int cls = 0; cls < 2; cls++) {
+    uint32_t counter = 0;
+    g_bargs.tasks = tasks[cls].data(); g_bargs.ntasks = (uint32_t)tasks[cls].size(); g_bargs.counter = &counter;
+    g_bargs.warp_words = class_warp_words(cls);
+    const int threads = cls == 0 ? ClassShape<0>::threads : ClassShape<1>::threads;
+    blockDim.x = threads; gridDim.x = blocks;
+    const size_t words = (size_t)(threads / 32) * g_bargs.warp_words;
+    std::vector<uint32_t> smem(words + 64, 0x5A5A5A5Au);
+    g_smem = smem.data();
+    for (int b = 0; b < blocks; b++) {
+      std::vector<GroupCtx> groups(threads / G);
+      for (auto &c : groups) c.bar.lanes = G;
+      g_cta_bar.lanes = threads;
+      std::vector<std::thread> ts;
+      for (int t = 0; t < threads; t++)
+        ts.emplace_back(cls == 0 ? dispatch_thread<0> : dispatch_thread<1>, (uint32_t)t, (uint32_t)b, groups.data(), G);
+      for (auto &t : ts) t.join();
+    }
+    if (counter < g_bargs.ntasks) { fprintf(stderr, "tasks left in the queue\n"); std::_Exit(6); }
+    for (size_t i = words; i < words + 64; i++)
+      if (smem[i] != 0x5A5A5A5Au) { fprintf(stderr, "shared memory overrun\n"); std::_Exit(4); }
+  }
+  return 0;
+}
 static uint32_t *alloc_words(size_t count) {
   return static_cast<uint32_t *>(aligned_alloc(64, ((count * 4 + 63) / 64) * 64 + 64));
 }
@@ -195,7 +257,14 @@ int main() {
     g_args.b_exps = be; g_args.b_limbs = b; g_args.c_exps = ce; g_args.c_limbs = c; g_args.err = &err;
     const int threads = 32 * warps, key = (G * 10000 + K * 100 + R) * 100 + op;
     int results = count;
-    if (op >= 50) {                              // register add/sub kernel: op 50 + OP
+    if (op == 60) {                              // mixed batch through the class kernels' dispatcher
+      std::vector<fpa_batch_desc> descs(count);
+      g_bargs = BatchArgs{};
+      g_bargs.r_exps = re; g_bargs.r_limbs = r; g_bargs.a_exps = ae; g_bargs.a_limbs = a;
+      g_bargs.b_exps = be; g_bargs.b_limbs = b; g_bargs.err = &err;
+      const int cfg = G == 4 ? 0 : (G == 8 ? 2 : 12);
+      if (run_dispatch(cfg, G, n, mode, count, blocks, ce, descs)) return 2;
+    } else if (op >= 50) {                       // register add/sub kernel: op 50 + OP
       switch (key - (op - 50)) {
 @REGK_CASES@        default: return 2;
       }
@@ -275,10 +344,23 @@ def cta_source():
     gh = open(os.path.join(CSRC, "..", "..", "include", "fpa_gb300.h")).read()
     desc = gh[gh.index("typedef struct {\n  uint8_t op;"):gh.index("} fpa_batch_desc;") + len("} fpa_batch_desc;")]
     bh = open(os.path.join(CSRC, "fpa_batch.h")).read()
-    structs = bh[bh.index("struct BatchTask {"):bh.index("// Tile width K of configuration")]
+    structs = _host_qualifiers(bh[bh.index("struct BatchTask {"):bh.index("// threads per CTA of each class kernel")])
     body = body.replace("template <int G>\nstruct Grp {", "}  // namespace gfpa\n" + desc + "\n" + structs
                         + "namespace gfpa {\ntemplate <int G>\nstruct Grp {", 1)
     body += "namespace gfpa {\n" + _host_qualifiers(task) + "}  // namespace gfpa\n"
+    # the class kernels' task dispatcher, its task list cut down to the configurations here
+    disp = bk[bk.index("#define GFPA_TASK_OP"):bk.index("}  // namespace gfpa\n\n#define GFPA_CAT2")]
+    tile4 = disp[disp.index("#define GFPA_TASKS_TILE4"):disp.index("template <int CLS>\nstruct ClassShape")]
+    disp = disp.replace(tile4, "#define GFPA_TASKS_TILE4 GFPA_TASK(0, 4, 2, 1) GFPA_TASK(2, 8, 4, 1) GFPA_TASK(12, 16, 4, 2)\n\n")
+    for old in ("GFPA_TASK(5, 32, 8, 1) GFPA_TASK(7, 16, 8, 1) GFPA_TASK(13, 8, 8, 4) GFPA_TASK(14, 16, 8, 2)",
+                "GFPA_TASK(6, 32, 16, 1) GFPA_TASK(8, 8, 16, 1) GFPA_TASK(9, 16, 16, 1)"):
+        assert disp.count(old) == 1
+        disp = disp.replace(old, "")
+    head = "__global__ void __launch_bounds__(ClassShape<CLS>::threads, ClassShape<CLS>::min_blocks)"
+    assert disp.count(head) == 1 and disp.count("__shared__ uint32_t s_task;") == 1
+    disp = disp.replace(head, "void").replace("__shared__ uint32_t s_task;", "static uint32_t s_task;")
+    disp = disp.replace("extern __shared__ __align__(16) uint32_t smem[];", "uint32_t *smem = g_smem;")
+    body += "namespace gfpa {\n" + _host_qualifiers(disp) + "}  // namespace gfpa\n"
     # the fused chains (fpa_chain.cu)
     ch = open(os.path.join(CSRC, "fpa_chain.cu")).read()
     chain = _host_qualifiers(ch[ch.index("struct ChainArgs {"):ch.index("template <int G, int K, int R>\ncudaError_t launch_chain")])
@@ -485,3 +567,50 @@ def test_register_addsub_kernel_matches_oracle(cta_binary, shape, n, op):
         ee, el = oracle.run(op, n, mode, *case[:4])
         assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
         assert np.array_equal(gl[ee > 8], el[ee > 8]), (op, n, mode)
+
+
+@pytest.mark.parametrize("shape,n,blocks", [((4, 2, 1), 5, 2), ((8, 4, 1), 17, 1), ((16, 4, 2), 100, 1)])
+def test_batch_dispatcher_matches_oracle(cta_binary, shape, n, blocks):
+    """k_batch (fpa_batch_kernels.cu) for register classes 0 and 1: CTAs of the class's size
+    take tasks from the queue through a shared word between two CTA barriers until it is
+    empty, each task a run of up to 7 same-op operations of a mixed batch (add, sub, mul,
+    div, sqrt interleaved in runs).  Every result is checked against the oracle."""
+    rng = np.random.default_rng(11000 + n)
+    sets = {0: addsub_cases(rng, n), 2: mul_cases(rng, n), 3: div_cases(rng, n), 4: sqrt_cases(rng, n)}
+    sets[1] = sets[0]
+    per = 12 if n < 64 else 5
+    ops = np.array([op for _ in range(3) for op in (0, 3, 2, 4, 1) for _ in range(per // 3 + 1)], np.uint32)
+    picks = {op: _sample(sets[op], int((ops == op).sum()) + 1) for op in range(5)}   # _sample keeps an even count
+    used = {op: 0 for op in range(5)}
+    rows = []
+    for op in ops:
+        c = picks[op]
+        k = used[op]; used[op] += 1
+        rows.append((c[0][k], c[1][k], c[2][k] if op != 4 else 0, c[3][k] if op != 4 else np.zeros(n, np.uint32)))
+    ae = np.array([r[0] for r in rows], np.uint32); al = np.stack([r[1] for r in rows])
+    be = np.array([r[2] for r in rows], np.uint32); bl = np.stack([r[3] for r in rows])
+    for mode in (0, 3):
+        err, ge, gl = run_cta(cta_binary, shape, 60, n, mode, (ae, al, be, bl, ops, np.zeros_like(al)), 1, blocks)
+        assert err == 0
+        for op in range(5):
+            m = ops == op
+            ee, el = oracle.run(op, n, mode, ae[m], al[m], be[m], bl[m]) if op != 4 else oracle.run(op, n, mode, ae[m], al[m])
+            assert np.array_equal(ge[m], ee), (op, n, mode)
+            assert np.array_equal(gl[m][ee > 8], el[ee > 8]), (op, n, mode)
+
+
+def test_batch_dispatcher_has_no_races(cta_tsan_binary, monkeypatch):
+    """The dispatcher's shared task word under ThreadSanitizer: thread 0 writes it, every
+    thread reads it between the two CTA barriers, and the next write comes after both."""
+    monkeypatch.setenv("TSAN_OPTIONS", "halt_on_error=1 exitcode=66")
+    n = 5
+    rng = np.random.default_rng(11100)
+    a = _sample(addsub_cases(rng, n), 24)
+    d = _sample(div_cases(rng, n), 24)
+    ops = np.array([0] * 10 + [3] * 10 + [1] * 10 + [4] * 10, np.uint32)
+    ae = np.concatenate([a[0][:10], d[0][:10], a[0][10:20], d[0][10:20]])
+    al = np.concatenate([a[1][:10], d[1][:10], a[1][10:20], d[1][10:20]])
+    be = np.concatenate([a[2][:10], d[2][:10], a[2][10:20], d[2][10:20]])
+    bl = np.concatenate([a[3][:10], d[3][:10], a[3][10:20], d[3][10:20]])
+    err, _, _ = run_cta(cta_tsan_binary, (4, 2, 1), 60, n, 3, (ae, al, be, bl, ops, np.zeros_like(al)), 1, 2)
+    assert err == 0
