@@ -1,15 +1,18 @@
-"""The elementwise kernel k_elementwise (cubigfloat_gb300/csrc/fpa_kernels.cu) for div, sqrt
-and fma, compiled for the host and run as whole CTAs: one host thread per GPU thread, each
-lane group with its own emulated collectives (as in test_group_ops_host.py), the CTA's
-shared memory one host buffer, and __syncthreads() a CTA barrier that also checks where it
-is called from.  The div/sqrt/fma loop makes every thread of a CTA run the same number of
-iterations and meet one CTA barrier per iteration, including the groups whose operation
-index is past the end.  On the GPU, bar.sync must be reached by all lanes of a warp at the
-same instruction; lanes that diverge onto two different barrier sites hang the CTA.  So the
-emulated barrier ends the program when two lanes of one warp arrive from different source
-lines, and a thread that skips a barrier makes the others time out.  Grids of 1 to 3 CTAs
-with 1, 2 or 4 warps per CTA, at operation counts that leave partial last iterations, are
-checked bit-exact against the oracle."""
+"""The kernels of the path compiled for the host and run as whole CTAs: the elementwise
+kernel k_elementwise (cubigfloat_gb300/csrc/fpa_kernels.cu) for all six operations, the
+batch kernels' task loop and dispatcher, both chain kernels, the row kernel and the register
+add/sub kernel.  Each GPU thread is a host thread; each lane group has its own emulated
+collectives (as in test_group_ops_host.py); the CTA's shared memory is one host buffer; and
+__syncthreads() is a CTA barrier that also checks where it is called from.
+
+The div/sqrt/fma loop makes every thread of a CTA run the same number of iterations and
+meet one CTA barrier per iteration, including the groups whose operation index is past the
+end.  On the GPU, bar.sync must be reached by all lanes of a warp at the same instruction;
+lanes that diverge onto two different barrier sites hang the CTA.  So the emulated barrier
+ends the program when two lanes of one warp arrive from different source lines, and a
+thread that skips a barrier makes the others time out.  Grids of 1 to 3 CTAs with 1, 2 or
+4 warps per CTA, at operation counts that leave partial last iterations, are checked
+bit-exact against the oracle."""
 import os
 import shutil
 import subprocess
@@ -323,7 +326,7 @@ int main() {
 """
 
 SHAPES = [(4, 2, 1), (8, 4, 1), (16, 4, 2)]
-OPS = (3, 4, 5)                    # div, sqrt, fma
+OPS = (0, 1, 2, 3, 4, 5)           # add, sub, mul (double-buffered loops), div, sqrt, fma (lockstep loop)
 
 
 def cta_source():
@@ -434,13 +437,16 @@ GRIDS = [((4, 2, 1), 5, 1, 2, 37), ((4, 2, 1), 8, 2, 3, 61), ((8, 4, 1), 17, 4, 
 @pytest.mark.parametrize("shape,n,warps,blocks,count", GRIDS)
 @pytest.mark.parametrize("op", OPS)
 def test_elementwise_kernel_lockstep_matches_oracle(cta_binary, shape, n, warps, blocks, count, op):
+    """k_elementwise on grids of emulated CTAs: add/sub/mul through the grid-stride
+    double-buffered loops, div/sqrt/fma through the lockstep loop."""
     rng = np.random.default_rng(10100 + 10 * n + op)
-    case = {3: div_cases, 4: sqrt_cases}[op](rng, n) if op != 5 else fma_cases(10200 + n, n)
+    make = {0: addsub_cases, 1: addsub_cases, 2: mul_cases, 3: div_cases, 4: sqrt_cases}
+    case = make[op](rng, n) if op != 5 else fma_cases(10200 + n, n)
     case = _sample(case, count)
     for mode in (0, 3, 4):
         err, ge, gl = run_cta(cta_binary, shape, op, n, mode, case, warps, blocks)
         ee, el = oracle.run_fma(n, mode, *case) if op == 5 else (
-            oracle.run(op, n, mode, *case[:4]) if op == 3 else oracle.run(op, n, mode, *case[:2]))
+            oracle.run(op, n, mode, *case[:4]) if op != 4 else oracle.run(op, n, mode, *case[:2]))
         assert err == 0
         assert np.array_equal(ge, ee), (op, n, mode, int(np.flatnonzero(ge != ee)[0]))
         val = ee > 8
