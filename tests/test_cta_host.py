@@ -128,7 +128,8 @@ static void run_chain(int threads, int blocks) {
     for (auto &c : groups) c.bar.lanes = G;
     g_cta_bar.lanes = threads;
     std::vector<std::thread> ts;
-    for (int t = 0; t < threads; t++) ts.emplace_back(chain_thread<KIND, G, K, R>, (uint32_t)t, (uint32_t)b, groups.data());
+    for (int t = 0; t < threads; t++)
+      ts.emplace_back(chain_thread<KIND, G, K, R>, (uint32_t)t, (uint32_t)b, groups.data());
     for (auto &t : ts) t.join();
   }
   for (size_t i = words; i < words + 64; i++)
@@ -354,7 +355,8 @@ def cta_source():
     # the class kernels' task dispatcher, its task list cut down to the configurations here
     disp = bk[bk.index("#define GFPA_TASK_OP"):bk.index("}  // namespace gfpa\n\n#define GFPA_CAT2")]
     tile4 = disp[disp.index("#define GFPA_TASKS_TILE4"):disp.index("template <int CLS>\nstruct ClassShape")]
-    disp = disp.replace(tile4, "#define GFPA_TASKS_TILE4 GFPA_TASK(0, 4, 2, 1) GFPA_TASK(2, 8, 4, 1) GFPA_TASK(12, 16, 4, 2)\n\n")
+    subset = "#define GFPA_TASKS_TILE4 GFPA_TASK(0, 4, 2, 1) GFPA_TASK(2, 8, 4, 1) GFPA_TASK(12, 16, 4, 2)\n\n"
+    disp = disp.replace(tile4, subset)
     for old in ("GFPA_TASK(5, 32, 8, 1) GFPA_TASK(7, 16, 8, 1) GFPA_TASK(13, 8, 8, 4) GFPA_TASK(14, 16, 8, 2)",
                 "GFPA_TASK(6, 32, 16, 1) GFPA_TASK(8, 8, 16, 1) GFPA_TASK(9, 16, 16, 1)"):
         assert disp.count(old) == 1
@@ -366,7 +368,8 @@ def cta_source():
     body += "namespace gfpa {\n" + _host_qualifiers(disp) + "}  // namespace gfpa\n"
     # the fused chains (fpa_chain.cu)
     ch = open(os.path.join(CSRC, "fpa_chain.cu")).read()
-    chain = _host_qualifiers(ch[ch.index("struct ChainArgs {"):ch.index("template <int G, int K, int R>\ncudaError_t launch_chain")])
+    chain = _host_qualifiers(ch[ch.index("struct ChainArgs {"):
+                                ch.index("template <int G, int K, int R>\ncudaError_t launch_chain")])
     assert chain.count("__global__ void __launch_bounds__(128, 4)") == 2
     chain = chain.replace("__global__ void __launch_bounds__(128, 4)", "void")
     chain = chain.replace("extern __shared__ __align__(16) uint32_t smem[];", "uint32_t *smem = g_smem;")
@@ -386,8 +389,8 @@ def cta_source():
     head = "__global__ void __launch_bounds__(128, (K <= 4) ? 8 : (K <= 8 ? 4 : 2))"
     assert regk.count(head) == 1
     body += "namespace gfpa {\n" + regk.replace(head, "void") + "}  // namespace gfpa\n"
-    cases = "".join(f"      case {(G * 10000 + K * 100 + R) * 100 + op}: run_grid<{op}, {G}, {K}, {R}>(threads, blocks); "
-                    f"break;\n" for (G, K, R) in SHAPES for op in OPS)
+    cases = "".join(f"      case {(G * 10000 + K * 100 + R) * 100 + op}: "
+                    f"run_grid<{op}, {G}, {K}, {R}>(threads, blocks); break;\n" for (G, K, R) in SHAPES for op in OPS)
     bcases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 20 + op}: run_batch_task<{op}, {G}, {K}, {R}>"
                      f"(threads, (uint32_t)count); break;\n" for (G, K, R) in SHAPES for op in range(5))
     ccases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 30 + kind}: run_chain<{kind}, {G}, {K}, {R}>"
@@ -395,7 +398,8 @@ def cta_source():
     rcases = "".join(f"        case {(G * 10000 + K * 100 + R) * 100 + 50}: "
                      f"if (op == 50) run_regk<OP_ADD, {G}, {K}>(threads, blocks); "
                      f"else run_regk<OP_SUB, {G}, {K}>(threads, blocks); break;\n" for (G, K, R) in SHAPES)
-    return body + MAIN.replace("@REGK_CASES@", rcases).replace("@CASES@", cases).replace("@BATCH_CASES@", bcases).replace("@CHAIN_CASES@", ccases)
+    main = MAIN.replace("@REGK_CASES@", rcases).replace("@CASES@", cases)
+    return body + main.replace("@BATCH_CASES@", bcases).replace("@CHAIN_CASES@", ccases)
 
 
 def build(src_text, path, flags):
@@ -404,8 +408,8 @@ def build(src_text, path, flags):
         pytest.skip("g++ not found")
     src, exe = path / "cta.cpp", path / "cta"
     src.write_text(src_text)
-    r = subprocess.run([cxx] + flags + ["-std=c++20", "-fno-strict-aliasing", "-pthread", "-w", "-o", str(exe), str(src)],
-                       capture_output=True, text=True)
+    r = subprocess.run([cxx] + flags + ["-std=c++20", "-fno-strict-aliasing", "-pthread", "-w", "-o", str(exe),
+                                        str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
     return str(exe)
 
@@ -453,7 +457,8 @@ def test_elementwise_kernel_lockstep_matches_oracle(cta_binary, shape, n, warps,
         assert np.array_equal(gl[val], el[val]), (op, n, mode)
 
 
-@pytest.mark.parametrize("shape,n,warps,count", [((4, 2, 1), 5, 2, 37), ((8, 4, 1), 17, 4, 29), ((16, 4, 2), 128, 2, 9)])
+@pytest.mark.parametrize("shape,n,warps,count", [((4, 2, 1), 5, 2, 37), ((8, 4, 1), 17, 4, 29),
+                                                 ((16, 4, 2), 128, 2, 9)])
 @pytest.mark.parametrize("op", range(5))
 def test_batch_task_lockstep_matches_oracle(cta_binary, shape, n, warps, count, op):
     """run_task (fpa_batch_kernels.cu): one task of `count` operations on one CTA of several
@@ -560,7 +565,8 @@ def test_row_kernel_matches_oracle(cta_binary, op, n):
         assert np.array_equal(gl[ee > 8], el[ee > 8]), (op, n, mode)
 
 
-@pytest.mark.parametrize("shape,n", [((4, 2, 1), 8), ((4, 2, 1), 5), ((8, 4, 1), 32), ((8, 4, 1), 19), ((16, 4, 2), 64)])
+@pytest.mark.parametrize("shape,n", [((4, 2, 1), 8), ((4, 2, 1), 5), ((8, 4, 1), 32), ((8, 4, 1), 19),
+                                     ((16, 4, 2), 64)])
 @pytest.mark.parametrize("op", [0, 1])
 def test_register_addsub_kernel_matches_oracle(cta_binary, shape, n, op):
     """k_addsub_regk (fpa_addsub_regs.cuh) as emulated CTAs of four warps on a grid of two:
@@ -600,7 +606,8 @@ def test_batch_dispatcher_matches_oracle(cta_binary, shape, n, blocks):
         assert err == 0
         for op in range(5):
             m = ops == op
-            ee, el = oracle.run(op, n, mode, ae[m], al[m], be[m], bl[m]) if op != 4 else oracle.run(op, n, mode, ae[m], al[m])
+            ee, el = (oracle.run(op, n, mode, ae[m], al[m], be[m], bl[m]) if op != 4
+                      else oracle.run(op, n, mode, ae[m], al[m]))
             assert np.array_equal(ge[m], ee), (op, n, mode)
             assert np.array_equal(gl[m][ee > 8], el[ee > 8]), (op, n, mode)
 

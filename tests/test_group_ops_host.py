@@ -1,14 +1,17 @@
-"""The lane-group add/sub, mul, div, sqrt and fma (op_addsub, op_mul, op_div, op_sqrt, op_fma in
-cubigfloat_gb300/csrc/fpa_ops.cuh, with every building block of fpa_device.cuh under them), compiled for the host from the device
-source and run on an emulated lane group: G host threads, one per lane, sharing the group's
-workspace as the kernel's shared-memory slice.  Each warp collective becomes publish -> group
-barrier -> read, and the group sync (__syncwarp) becomes the barrier alone; the few inline
-PTX carry chains get host equivalents.  Results are checked bit-exact against the oracle in
-every rounding mode on random operands, near-halfway / near-exact cases, all-ones mantissas
-and the special classes (fma: the seeded fma cases with cancellation, and every class
-combination), for the lane-group shapes of the launcher's configuration table at
-sizes from one limb up to the group's capacity.  A div/sqrt internal check that fails sets
-the error word, which must stay 0.  The GPU tests run the same functions in the kernels."""
+"""The lane-group add/sub, mul, div, sqrt and fma (op_addsub, op_mul, op_div, op_sqrt, op_fma
+in cubigfloat_gb300/csrc/fpa_ops.cuh, with every building block of fpa_device.cuh under
+them) and the elementwise kernels' double-buffered add/sub and mul loops, compiled for the
+host from the device source and run on an emulated lane group: G host threads, one per
+lane, sharing the group's workspace as the kernel's shared-memory slice.  Each warp
+collective becomes publish -> group barrier -> read, and the group sync (__syncwarp)
+becomes the barrier alone; the few inline PTX carry chains get host equivalents.  Results
+are checked bit-exact against the oracle in every rounding mode on random operands,
+near-halfway / near-exact cases, all-ones mantissas and the special classes (fma: the
+seeded fma cases with cancellation, and every class combination), for the lane-group
+shapes the tuned table uses, at sizes from one limb up to the group's capacity.  A div/sqrt
+internal check that fails sets the error word, which must stay 0.  A ThreadSanitizer build
+checks that lanes touch shared words only in an order the syncs and collectives fix.  The
+GPU tests run the same functions in the kernels."""
 import os
 import re
 import shutil
@@ -321,7 +324,8 @@ def host_source():
     dev = _replace_once(dev, "__device__ __forceinline__ void mac3(", '"r"(a), "r"(b));\n}\n', HOST_MAC3)
     dev = _replace_once(dev, 'asm("sub.cc.u32', '"r"(a0), "r"(a1), "r"(a2));',
                         "sub3(lo[c], hi[c], tp[c], a0, a1, a2);")
-    args = launch[launch.index("struct ElementwiseArgs {"):launch.index("};", launch.index("struct ElementwiseArgs {")) + 3]
+    at = launch.index("struct ElementwiseArgs {")
+    args = launch[at:launch.index("};", at) + 3]
     pipe = kern[kern.index("// add/sub: HBM-bound"):kern.index("// sqrt may run CTAs")]
     body = dev + "\n" + ops + "\nnamespace gfpa {\n" + pipe + "}  // namespace gfpa\n"
     body = args + body
