@@ -8,13 +8,21 @@ Inputs (541 MB per operand array) are larger than L2, so no flush is needed.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl gb300|reference]
 
+After the timed region every result of the step is checked bit-exact against the oracle
+(the exact-integer C restatement, on all host cores), which also gives the CPU baseline;
+MPFR runs on a sample beside it.  The other workloads (1024-bit add/mul, the 10^6-op mixed
+batch, the chains, the served stream, the reference's own kernels) are measured and
+checked in `extras`.
+
 --impl reference times the reference path's CPU implementation (the oracle's C
-restatement) on the host cores over a bounded sample of the same workload.
+restatement; the reference itself has none) on the host cores over a bounded sample of the
+same workload, one third each mul, div and sqrt like the GPU step.
 Under torchrun each rank runs an independent replica (the operation shards trivially by
 index with no exchange); rank 0 prints one JSON line.
 """
 import argparse
 import ctypes
+import hashlib
 import json
 import os
 import subprocess
@@ -35,7 +43,8 @@ OP_CODE = {"add": 0, "sub": 1, "mul": 2, "div": 3, "sqrt": 4}
 # mul n^2, div n^2, sqrt n^2/2; two integer multiply-adds (lo, hi) per product
 PRODUCTS = {"mul": N_LIMBS ** 2, "div": N_LIMBS ** 2, "sqrt": N_LIMBS ** 2 // 2}
 METRIC = "bit-exact mul/div/sqrt ops/s at 4096 bits (2^20 operands each)"
-CPU_SAMPLE = {"mul": 131072, "div": 131072, "sqrt": 32768}
+REF_SAMPLE = 32768          # reference arm: operands per operation per step (mul:div:sqrt = 1:1:1)
+MPFR_SAMPLE = 16384         # MPFR: operands per operation (1:1:1), split over the host cores
 
 
 def parse():
@@ -123,35 +132,63 @@ def make_inputs(count, seed=20240):
     return data
 
 
-def cpu_leg(data, gpu_results, threads):
-    """Oracle (C restatement, all host threads) on a bounded sample of the same operands;
-    also checks the GPU results on that sample."""
+def canonical(e, l):
+    """Result arrays with the limbs of class results zeroed (those limbs are unspecified)."""
+    e = np.ascontiguousarray(e, dtype=np.uint32)
+    l = np.array(l, dtype=np.uint32).reshape(e.size, -1)
+    l[e <= 8] = 0
+    return e, l
+
+
+def sha256_of(e, l):
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(e, dtype=np.uint32).tobytes())
+    h.update(np.ascontiguousarray(l, dtype=np.uint32).tobytes())
+    return h.hexdigest()
+
+
+def equal_mix_rate(rates):
+    """ops/s of a step doing the same number of each operation, from per-operation rates"""
+    return len(rates) / sum(1.0 / r for r in rates)
+
+
+def cpu_leg(data, gpu_results, threads, count=None):
+    """The oracle (exact-integer C restatement, `threads` host threads) over the first `count`
+    operands of each operation (all by default) -- the CPU baseline at the GPU step's 1:1:1
+    mix -- and, when GPU results are given, the bit-exact check of every one of them."""
     import oracle
-    total_ops, total_s, exact = 0, 0.0, True
-    per = {}
+    per, secs, exact, shas = {}, {}, {}, {}
     for op in OPS:
         (ae, al), (be, bl) = data[op]
-        k = min(CPU_SAMPLE[op], len(ae))
+        k = len(ae) if count is None else min(count, len(ae))
         t0 = time.perf_counter()
         re_, rl = oracle.run(OP_CODE[op], N_LIMBS, 3, ae[:k], al[:k], be[:k], bl[:k], threads=threads)
         dt = time.perf_counter() - t0
-        total_ops += k
-        total_s += dt
-        per[op] = k / dt
+        per[op], secs[op] = k / dt, dt
         if gpu_results is not None:
-            ge, gl = gpu_results[op]
-            val = re_ > 8
-            ok = np.array_equal(ge[:k], re_) and np.array_equal(gl[:k][val], rl[val])
-            exact = exact and ok
-    return {"value": total_ops / total_s, "unit": "ops/s", "cores": threads, "kind": "port",
-            "sample": "first {} mul, {} div, {} sqrt operands of the same 4096-bit workload, ties-to-even".format(
-                CPU_SAMPLE["mul"], CPU_SAMPLE["div"], CPU_SAMPLE["sqrt"]),
-            "per_op_ops_s": {k: round(v, 1) for k, v in per.items()},
-            "gpu_sample_bit_exact": exact if gpu_results is not None else None}
+            ge, gl = canonical(gpu_results[op][0][:k], gpu_results[op][1][:k])
+            oe, ol = canonical(re_, rl)
+            exact[op] = bool(np.array_equal(ge, oe) and np.array_equal(gl, ol))
+            shas[op] = sha256_of(oe, ol) if exact[op] else {"oracle": sha256_of(oe, ol), "gpu": sha256_of(ge, gl)}
+    k = len(data[OPS[0]][0][0]) if count is None else count
+    cpu = {"value": equal_mix_rate(list(per.values())), "unit": "ops/s", "cores": threads, "kind": "port",
+           "sample": ("all 2^20 operands of each of mul, div, sqrt" if count is None else
+                      f"the first {k} operands of each of mul, div, sqrt") +
+                     " of the same 4096-bit workload, ties-to-even, one third each (the GPU step's mix)",
+           "seconds": round(sum(secs.values()), 2),
+           "per_op_ops_s": {o: round(v, 1) for o, v in per.items()}}
+    check = None
+    if gpu_results is not None:
+        check = {"ok": all(exact.values()), "checked_ops": 3 * k, "of_ops": 3 * len(data[OPS[0]][0][0]),
+                 "against": "oracle (exact integers; pinned to MPFR 4.2.1)", "per_op": exact,
+                 "sha256": shas}
+    return cpu, check
 
 
-def mpfr_leg(data, threads):
-    """MPFR 4.2.1 (the reference's test oracle) on the host, single thread, same sample."""
+def mpfr_leg(data, gpu_results, threads, count=MPFR_SAMPLE):
+    """MPFR 4.2.1 (the reference's test oracle) on the host cores: the first `count` operands
+    of each operation split into `threads` chunks run concurrently; also checks the GPU
+    results on that sample against MPFR."""
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
     try:
         import gold
@@ -159,18 +196,26 @@ def mpfr_leg(data, threads):
             return None
     except Exception:
         return None
-    per, tot_ops, tot_s = {}, 0, 0.0
+    from concurrent.futures import ThreadPoolExecutor
+    per, exact = {}, True
     for op in OPS:
         (ae, al), (be, bl) = data[op]
-        k = min(CPU_SAMPLE[op], len(ae))
+        k = min(count, len(ae))
+        bounds = np.linspace(0, k, threads + 1).astype(int)
+        parts = [(lo, hi) for lo, hi in zip(bounds[:-1], bounds[1:]) if hi > lo]
         t0 = time.perf_counter()
-        gold.run(OP_CODE[op], N_LIMBS, 3, ae[:k], al[:k], be[:k], bl[:k])
-        dt = time.perf_counter() - t0
-        per[op] = k / dt
-        tot_ops += k
-        tot_s += dt
-    return {"value": tot_ops / tot_s, "unit": "ops/s", "cores": 1, "kind": "mpfr",
-            "per_op_ops_s": {k: round(v, 1) for k, v in per.items()}, "version": gold.version()}
+        with ThreadPoolExecutor(max_workers=len(parts)) as ex:
+            res = list(ex.map(lambda lh: gold.run(OP_CODE[op], N_LIMBS, 3, ae[lh[0]:lh[1]], al[lh[0]:lh[1]],
+                                                  be[lh[0]:lh[1]], bl[lh[0]:lh[1]]), parts))
+        per[op] = k / (time.perf_counter() - t0)
+        if gpu_results is not None:
+            me, ml = canonical(np.concatenate([r[0] for r in res]), np.concatenate([r[1] for r in res]))
+            ge, gl = canonical(gpu_results[op][0][:k], gpu_results[op][1][:k])
+            exact = exact and bool(np.array_equal(me, ge) and np.array_equal(ml, gl))
+    return {"value": equal_mix_rate(list(per.values())), "unit": "ops/s", "cores": threads, "kind": "mpfr",
+            "sample": f"the first {count} operands of each of mul, div, sqrt, one third each",
+            "per_op_ops_s": {o: round(v, 1) for o, v in per.items()}, "version": gold.version(),
+            "gpu_sample_bit_exact_vs_mpfr": exact if gpu_results is not None else None}
 
 
 def load_traffic():
@@ -185,22 +230,26 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    count = min(args.count, max(CPU_SAMPLE.values()))
+    count = min(args.count, REF_SAMPLE)
     data = make_inputs(count)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_leg(data, None, threads)
-    vals = []
+        cpu_leg(data, None, threads, count)
+    steps = []
     for _ in range(args.steps):
-        vals.append(cpu_leg(data, None, threads)["value"])
-    v = float(np.median(vals))
-    cb = cpu_leg(data, None, threads)
+        t0 = time.perf_counter()
+        cb, _ = cpu_leg(data, None, threads, count)
+        steps.append((time.perf_counter() - t0, cb))
+    ms_step = float(np.median([t for t, _ in steps])) * 1e3
+    v = len(OPS) * count / (ms_step / 1e3)
+    cb = dict(steps[-1][1])
     cb["value"] = v
     line = {"metric": METRIC, "value": v, "unit": "ops/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": "4096-bit mul/div/sqrt, 2^20 operands each", "limbs": N_LIMBS, "sample_ops":
-                       sum(min(CPU_SAMPLE[o], count) for o in OPS), "mode": "ties_to_even"},
+            "config": {"workload": "4096-bit mul/div/sqrt, 2^20 operands each", "limbs": N_LIMBS,
+                       "step": f"the first {count} operands of each of mul, div, sqrt (1:1:1, as the GPU step)",
+                       "sample_ops": len(OPS) * count, "mode": "ties_to_even"},
             "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -232,27 +281,46 @@ def _timed(torch, fn, reps=3):
     return e0.elapsed_time(e1) / reps
 
 
-def extra_add_mul_1024(fpa, torch, count=1 << 22):
-    """1024-bit add and mul (the 1024-bit workload's shape: uniform mantissas, e in [-64, 64],
-    random signs) over 2^22 pairs so that the operands (554 MB each) exceed L2; add is
-    HBM-bound, so its roofline is bytes moved per second against the copy bandwidth."""
+def extra_add_mul_1024(fpa, torch, roofline_count=1 << 22, count=65536):
+    """1024-bit add and mul (uniform mantissas, e in [-64, 64], random signs, ties-to-even).
+    At the stated 65,536 pairs the operands (8.6 MB) sit in L2 and a launch takes a few
+    microseconds, so that case is timed over back-to-back launches and every result is
+    checked bit-exact against the oracle; the HBM roofline of add is measured over 2^22
+    pairs (554 MB per operand array, larger than L2)."""
+    import oracle
     from cubigfloat_gb300 import workloads as W
     n = 32
+    peak, src = hbm_peak()
+    out = {}
     (ae, al), (be, bl) = W.workload_1024(11, count=count, n=n)
     A, B, R = fpa.FpaArray(count, 32 * n), fpa.FpaArray(count, 32 * n), fpa.FpaArray(count, 32 * n)
     A.to_device(ae, al)
     B.to_device(be, bl)
-    out = {}
-    peak, src = hbm_peak()
+    stated = {}
+    for name, fn in (("add", fpa.fpa_add), ("mul", fpa.fpa_mul)):
+        ms = _timed(torch, lambda: fn(R, A, B, fpa.fpa_round_ties_to_even), reps=200)
+        ge, gl = canonical(*R.to_host())
+        oe, ol = canonical(*oracle.run(OP_CODE[name], n, 3, ae, al, be, bl, threads=os.cpu_count() or 1))
+        ok = bool(np.array_equal(ge, oe) and np.array_equal(gl, ol))
+        stated[name] = {"ops_s": count / (ms / 1e3), "us_per_launch": ms * 1e3,
+                        "bit_exact": {"ok": ok, "checked_ops": count, "sha256": sha256_of(oe, ol)}}
+    out["stated_65536_pairs"] = stated
+    del A, B, R
+    (ae, al), (be, bl) = W.workload_1024(11, count=roofline_count, n=n)
+    A, B, R = (fpa.FpaArray(roofline_count, 32 * n), fpa.FpaArray(roofline_count, 32 * n),
+               fpa.FpaArray(roofline_count, 32 * n))
+    A.to_device(ae, al)
+    B.to_device(be, bl)
     for name, fn in (("add", fpa.fpa_add), ("mul", fpa.fpa_mul)):
         ms = _timed(torch, lambda: fn(R, A, B, fpa.fpa_round_ties_to_even))
-        rec = {"ops_s": count / (ms / 1e3), "ms": ms}
+        rec = {"ops_s": roofline_count / (ms / 1e3), "ms": ms}
         if name == "add":
-            gbs = 3 * count * (4 + 4 * n) / (ms / 1e3) / 1e9
+            gbs = 3 * roofline_count * (4 + 4 * n) / (ms / 1e3) / 1e9
             rec.update({"hbm_gbs": gbs, "hbm_peak_gbs": peak, "hbm_frac": gbs / peak, "peak_source": src})
-        out[name] = rec
+        out[f"{name}_{roofline_count}_pairs"] = rec
     del A, B, R
-    return {"workload": f"1024-bit add and mul, {count} pairs, ties-to-even", **out}
+    return {"workload": f"1024-bit add and mul, {count} pairs (checked) and {roofline_count} pairs (roofline), "
+                        "ties-to-even", **out}
 
 
 def extra_batched(fpa, torch, count):
@@ -296,36 +364,90 @@ def extra_batched(fpa, torch, count):
                                  g_bl.data_ptr() + 4 * lo)
             assert rc == 0, rc
     ms_plain = _timed(torch, plain)
-    re_b, rl_b = d_re.cpu().numpy(), d_rl.cpu().numpy()
-    re_p, rl_p = g_re.cpu().numpy(), g_rl.cpu().numpy()
+    re_b, rl_b = d_re.cpu().numpy().view(np.uint32), d_rl.cpu().numpy().view(np.uint32)
+    re_p, rl_p = g_re.cpu().numpy().view(np.uint32), g_rl.cpu().numpy().view(np.uint32)
     same_e = np.array_equal(re_b[order], re_p)
     valued = np.repeat(re_p > 8, lens)             # limbs are defined for ordinary values only
     same_l = np.array_equal(rl_b[r_sel][valued], rl_p[valued])
     tasks, _ = b.info()
     b.destroy()
+    # every result of the graph-launched batch against the oracle (checker, all host cores)
+    import oracle
+    t0 = time.perf_counter()
+    oe, ol = oracle.run_mixed(descs["op"], descs["limbs"], descs["mode"], ae, al, descs["a_off"], be, bl,
+                              descs["b_off"], descs["r_off"], total, threads=os.cpu_count() or 1)
+    check_s = time.perf_counter() - t0
+    r_all = np.repeat(descs["r_off"].astype(np.int64), descs["limbs"].astype(np.int64)) + (
+        np.arange(int(descs["limbs"].astype(np.int64).sum())) -
+        np.repeat(np.cumsum(descs["limbs"].astype(np.int64)) - descs["limbs"].astype(np.int64),
+                  descs["limbs"].astype(np.int64)))
+    val_all = np.repeat(oe > 8, descs["limbs"].astype(np.int64))
+    ok_e = np.array_equal(re_b, oe)
+    ok_l = np.array_equal(rl_b[r_all][val_all], ol[r_all][val_all])
+    ol_c = ol[r_all].copy()
+    ol_c[~val_all] = 0
     return {"workload": f"{count} mixed ops (add/sub/mul/div/sqrt 30/20/30/10/10), 256..16384 bits log-uniform",
             "ops_s_graph": count / (ms_graph / 1e3), "ms_graph": ms_graph, "ms_run": ms_run,
             "ops_s_plain_launches": count / (ms_plain / 1e3), "ms_plain": ms_plain, "plain_launches": len(groups),
             "speedup_vs_plain": ms_plain / ms_graph, "tasks_per_class": tasks,
-            "bit_identical_to_plain": bool(same_e and same_l)}
+            "bit_identical_to_plain": bool(same_e and same_l),
+            "bit_exact": {"ok": bool(ok_e and ok_l), "checked_ops": count, "against": "oracle",
+                          "check_s": round(check_s, 1), "sha256": sha256_of(oe, ol_c)}}
 
 
-def extra_chains(fpa, torch, dots=10000, length=1024, newtons=10000):
-    """Dot products (acc += x*y, each step rounded, 2048 bits) and Newton sqrt
-    (y <- (y + x/y)/2, 8 iterations at 8192 bits, x in [1, 2)), one launch each."""
+def _stepwise_dot(oracle, n, xe, xl, ye, yl, count, length, threads):
+    """acc = RN(acc + RN(x*y)) in order, every step a separate oracle operation"""
     from cubigfloat_gb300 import workloads as W
+    xl = xl.reshape(count, length, n)
+    yl = yl.reshape(count, length, n)
+    xe = xe.reshape(count, length)
+    ye = ye.reshape(count, length)
+    acc_e = np.full(count, W.CLS_ZERO, np.uint32)
+    acc_l = np.zeros((count, n), np.uint32)
+    for i in range(length):
+        te, tl = oracle.run(2, n, 3, xe[:, i], xl[:, i], ye[:, i], yl[:, i], threads=threads)
+        acc_e, acc_l = oracle.run(0, n, 3, acc_e, acc_l, te, tl, threads=threads)
+    return acc_e, acc_l
+
+
+def _stepwise_newton(oracle, n, xe, xl, ye, yl, iters, threads):
+    """y <- RN(RN(y + RN(x/y)) * 0.5), every step a separate oracle operation (the halving is
+    exact: the exponent word of a value drops by 2)"""
+    for _ in range(iters):
+        qe, ql = oracle.run(3, n, 3, xe, xl, ye, yl, threads=threads)
+        se, sl = oracle.run(0, n, 3, ye, yl, qe, ql, threads=threads)
+        ye, yl = np.where(se > 8, se - 2, se).astype(np.uint32), sl
+    return ye, yl
+
+
+def extra_chains(fpa, torch, dots=10000, length=1024, newtons=10000, check_dots=100):
+    """Dot products (acc += x*y, each step rounded, 2048 bits) and Newton sqrt
+    (y <- (y + x/y)/2, 8 iterations at 8192 bits, x in [1, 2)), one launch each; the first
+    `check_dots` dot products and every Newton chain are checked against the same operation
+    sequence run step by step in the oracle."""
+    import oracle
+    from cubigfloat_gb300 import workloads as W
+    threads = os.cpu_count() or 1
     rng = np.random.default_rng(4)
     n = 64
     xe, xl = W.uniform(rng, dots * length, n, -64, 64)
     ye, yl = W.uniform(rng, dots * length, n, -64, 64)
     dxe, dxl, dye, dyl = (_dev(torch, x) for x in (xe, xl, ye, yl))
-    del xl, yl
     re_ = torch.zeros(dots, dtype=torch.int32, device="cuda")
     rl = torch.zeros(dots * n, dtype=torch.int32, device="cuda")
     ms_dot = _timed(torch, lambda: fpa.dot(2048, dots, length, 3, re_.data_ptr(), rl.data_ptr(), dxe.data_ptr(),
                                            dxl.data_ptr(), dye.data_ptr(), dyl.data_ptr()), reps=2)
     del dxe, dxl, dye, dyl
     torch.cuda.empty_cache()
+    k = min(check_dots, dots)
+    t0 = time.perf_counter()
+    oe, ol = canonical(*_stepwise_dot(oracle, n, xe[:k * length], xl[:k * length], ye[:k * length],
+                                      yl[:k * length], k, length, threads))
+    ge, gl = canonical(re_.cpu().numpy().view(np.uint32)[:k], rl.cpu().numpy().view(np.uint32)[:k * n])
+    dot_check = {"ok": bool(np.array_equal(oe, ge) and np.array_equal(ol, gl)), "checked_chains": k,
+                 "of_chains": dots, "against": "oracle, step by step", "sha256": sha256_of(oe, ol),
+                 "check_s": round(time.perf_counter() - t0, 1)}
+    del xl, yl
     n2 = 256
     xl2 = rng.integers(0, 1 << 32, size=(newtons, n2), dtype=np.uint64).astype(np.uint32)
     xl2[:, -1] |= np.uint32(0x80000000)
@@ -342,10 +464,45 @@ def extra_chains(fpa, torch, dots=10000, length=1024, newtons=10000):
         assert fpa.newton_sqrt(8192, newtons, 8, 3, dye2.data_ptr(), dyl2.data_ptr(), dxe2.data_ptr(),
                                dxl2.data_ptr()) == 0
     ms_newton = _timed(torch, newton, reps=2)
+    t0 = time.perf_counter()
+    oe, ol = canonical(*_stepwise_newton(oracle, n2, xe2, xl2, xe2.copy(), y0, 8, threads))
+    ge, gl = canonical(dye2.cpu().numpy().view(np.uint32), dyl2.cpu().numpy().view(np.uint32))
+    newton_check = {"ok": bool(np.array_equal(oe, ge) and np.array_equal(ol, gl)), "checked_chains": newtons,
+                    "of_chains": newtons, "against": "oracle, step by step", "sha256": sha256_of(oe, ol),
+                    "check_s": round(time.perf_counter() - t0, 1)}
     return {"dot": {"workload": f"{dots} dot products of length {length} at 2048 bits",
-                    "ms": ms_dot, "mul_add_steps_s": dots * length / (ms_dot / 1e3)},
+                    "ms": ms_dot, "mul_add_steps_s": dots * length / (ms_dot / 1e3), "bit_exact": dot_check},
             "newton_sqrt": {"workload": f"{newtons} Newton sqrt(x), 8 iterations at 8192 bits",
-                            "ms": ms_newton, "iterations_s": newtons * 8 / (ms_newton / 1e3)}}
+                            "ms": ms_newton, "iterations_s": newtons * 8 / (ms_newton / 1e3),
+                            "bit_exact": newton_check}}
+
+
+def extra_reference_gpu(per_op_ms_ours, count=1 << 20):
+    """The reference's own kernels (its fpa.cu compiled for sm_103a, launched as its host
+    dispatcher does: one warp per number, 128-thread blocks) timed on this GPU with driver
+    events over the same 4096-bit operands as the timed step, and over 1024-bit add/mul;
+    beside each, our kernel's time on the same work."""
+    import oracle
+    if not oracle.ref_gpu_available():
+        return {"unavailable": "the reference's kernels were not compiled (no reference sources where built)"}
+    data = make_inputs(count)
+    out = {"launch": "reference fpa_kernel_warp_<op>_<size>, <<<ceil(32*count/128), 128>>>, repeat 3, mean"}
+    for op in OPS:
+        (ae, al), (be, bl) = data[op]
+        _, _, ms = oracle.ref_gpu_run(op, N_LIMBS, 3, ae, al, None if op == "sqrt" else be,
+                                      None if op == "sqrt" else bl, repeat=3)
+        rec = {"ms": round(ms, 3), "ops_s": count / (ms / 1e3)}
+        if op in per_op_ms_ours:
+            rec["ours_ms"] = round(per_op_ms_ours[op], 3)
+            rec["speedup_ours_over_reference"] = round(ms / per_op_ms_ours[op], 2)
+        out[f"{op}_4096"] = rec
+    del data
+    from cubigfloat_gb300 import workloads as W
+    (ae, al), (be, bl) = W.workload_1024(11, count=count, n=32)
+    for op in ("add", "mul"):
+        _, _, ms = oracle.ref_gpu_run(op, 32, 3, ae, al, be, bl, repeat=3)
+        out[f"{op}_1024"] = {"ms": round(ms, 3), "ops_s": count / (ms / 1e3)}
+    return out
 
 
 def extra_served(fpa, njobs=400, rates=(1000.0, 4000.0, 16000.0, None)):
@@ -386,16 +543,18 @@ def extra_served(fpa, njobs=400, rates=(1000.0, 4000.0, 16000.0, None)):
     return out
 
 
-EXTRAS = ("add_mul_1024", "batched_mixed", "chains", "served")
+EXTRAS = ("add_mul_1024", "batched_mixed", "chains", "served", "reference_gpu")
 
 
-def run_extras(fpa, torch, quick, only=EXTRAS):
+def run_extras(fpa, torch, quick, only=EXTRAS, per_op_ms=None):
     out = {}
     for name, fn in (("add_mul_1024", lambda: extra_add_mul_1024(fpa, torch, 1 << 20 if quick else 1 << 22)),
                      ("batched_mixed", lambda: extra_batched(fpa, torch, 100000 if quick else 1000000)),
                      ("chains", lambda: extra_chains(fpa, torch, dots=1000 if quick else 10000,
-                                                     newtons=1000 if quick else 10000)),
-                     ("served", lambda: extra_served(fpa, njobs=100 if quick else 400))):
+                                                     newtons=1000 if quick else 10000,
+                                                     check_dots=20 if quick else 100)),
+                     ("served", lambda: extra_served(fpa, njobs=100 if quick else 400)),
+                     ("reference_gpu", lambda: extra_reference_gpu(per_op_ms or {}, 1 << 18 if quick else 1 << 20))):
         if name not in only:
             continue
         t0 = time.perf_counter()
@@ -452,6 +611,7 @@ def run_gb300(args):
         step()
     torch.cuda.synchronize()
     lo, hi = fpa.measure_imad_peak()
+    prod_peak = fpa.measure_product_peak()
     clocks = Clocks(local)
     if world > 1:
         dist.barrier()
@@ -571,28 +731,34 @@ def run_gb300(args):
             dist.destroy_process_group()
         return
 
+    # roofline of the dominant kernel: algorithmic limb products (schoolbook-equivalent:
+    # mul n^2, div n^2, sqrt n^2/2 per operation) per CUDA-event second, against the measured
+    # limb-product rate of the kernels' own instruction triple
     dom = max(OPS, key=lambda o: per_op_ms[o])
-    alg_imad = 2 * PRODUCTS[dom] * count
-    achieved = alg_imad / (per_op_ms[dom] / 1e3) / 1e12
+    achieved = PRODUCTS[dom] * count / (per_op_ms[dom] / 1e3) / 1e12
     traffic = load_traffic().get(f"{dom}_n{n}")
     roofline = {"bound": "int-multiply", "kernel": f"k_elementwise<{dom}>, 4096-bit",
-                "achieved": round(achieved, 3), "peak": round(lo / 1e12, 3), "unit": "T IMAD/s",
-                "frac": round(achieved / (lo / 1e12), 4),
-                "peak_source": "measured live: mad.lo.u32 over all SMs (fpa_gb300_measure_imad_peak)",
-                "mad_hi_peak": round(hi / 1e12, 3),
+                "achieved": round(achieved, 4), "peak": round(prod_peak / 1e12, 4), "unit": "T limb products/s",
+                "frac": round(achieved / (prod_peak / 1e12), 4),
+                "peak_source": "measured live on this GPU: mad.lo.cc + madc.hi.cc + addc per 32x32-bit limb "
+                               "product into 96-bit columns, 8-column register tiles on every SM "
+                               "(fpa_gb300_measure_product_peak)",
+                "basis": f"{PRODUCTS[dom]} limb products per {dom} at {n} limbs x {count} operations per launch",
+                "isolated_instruction_peaks": {"mad_lo_T_per_s": round(lo / 1e12, 3), "mad_hi_T_per_s": round(hi / 1e12, 3)},
                 "traffic": traffic,
                 "per_op": {op: {"ms": round(per_op_ms[op], 3), "ops_s": round(count / (per_op_ms[op] / 1e3), 1),
-                                "imad_frac": round(2 * PRODUCTS[op] * count / (per_op_ms[op] / 1e3) / lo, 4)}
+                                "product_frac": round(PRODUCTS[op] * count / (per_op_ms[op] / 1e3) / prod_peak, 4)}
                            for op in OPS}}
+    cpu, bit_exact = None, None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cpu, bit_exact = cpu_leg(data, gpu_results, threads)
+        m = mpfr_leg(data, gpu_results, threads)
+        if m is not None:
+            cpu["mpfr"] = m
     extras = None
     if not args.no_extras and world == 1:
-        extras = run_extras(fpa, torch, args.quick_extras, args.extras.split(","))
-    cpu = None
-    if not args.no_cpu:
-        cpu = cpu_leg(data, gpu_results, os.cpu_count() or 1)
-        m = mpfr_leg(data, 1)
-        if m is not None:
-            cpu["mpfr_single_thread"] = m
+        extras = run_extras(fpa, torch, args.quick_extras, args.extras.split(","), per_op_ms)
     line = {"metric": METRIC, "value": value, "unit": "ops/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
@@ -600,7 +766,7 @@ def run_gb300(args):
                        "near_halfway_frac": 0.05, "mode": "ties_to_even", "step": "fpa_mul+fpa_div+fpa_sqrt",
                        "l2": "inputs 541 MB per operand array, larger than L2; no flush",
                        "parallelism": f"replicas x{world}"},
-            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "roofline": roofline, "cpu_baseline": cpu, "bit_exact": bit_exact, "clocks": clk,
             "e2e": {"value": e2e_val, "unit": "ops/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "api": "fpa_copy_array_to_device_async + fpa_op_async + fpa_copy_array_to_host_async "
                            "(pinned host buffers; copy-in, compute and copy-out on three streams)",

@@ -85,6 +85,7 @@ def lib():
         "fpa_gb300_get_config": (i32, [u32]),
         "fpa_gb300_version": (ctypes.c_char_p, []),
         "fpa_gb300_measure_imad_peak": (i32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+        "fpa_gb300_measure_product_peak": (i32, [ctypes.POINTER(ctypes.c_double)]),
         "fpa_batch_create": (i32, [ctypes.POINTER(vp), vp, u64]),
         "fpa_batch_run": (i32, [vp, vp, vp, vp, vp, vp, vp, vp]),
         "fpa_batch_capture": (i32, [vp, vp, vp, vp, vp, vp, vp]),
@@ -283,6 +284,16 @@ def measure_imad_peak():
     if rc != fpa_success:
         raise FpaError(f"fpa_gb300_measure_imad_peak -> {rc}")
     return lo.value, hi.value
+
+
+def measure_product_peak():
+    """Limb products per second (mad.lo.cc / madc.hi.cc / addc into 96-bit columns, the
+    product kernels' instruction triple) measured on the current GPU."""
+    p = ctypes.c_double()
+    rc = lib().fpa_gb300_measure_product_peak(ctypes.byref(p))
+    if rc != fpa_success:
+        raise FpaError(f"fpa_gb300_measure_product_peak -> {rc}")
+    return p.value
 
 
 def set_op_config(op, limbs, cfg):

@@ -14,19 +14,25 @@
 #include "fpa_launch.h"
 #include "fpa_misc.h"
 #include "fpa_batch.h"
+#include "fpa_devctx.h"
 
 namespace {
 
 struct State {
   std::mutex mu;
-  int device = -1;
-  int sms = 0;
-  uint32_t *err = nullptr;                // device error word
   // per operation and limb count: configuration + 1, 0 = default.  Zero-initialised (no
   // constructor), so the table is ready before any static initialiser of another file runs.
   int8_t cfg_override[5][GFPA_MAX_LIMBS + 1];
 };
 State g_state;
+
+// Per-device context: the SM count that sizes the grids and the device word the kernels
+// OR their error bits into, made on the first call that finds the device current.
+struct DevCtx {
+  int sms;
+  uint32_t *err;
+};
+PerDevice<DevCtx> g_dev;
 
 bool ctx(int &sms, uint32_t *&err);
 
@@ -54,20 +60,23 @@ int gfpa_cfg_for_op(int op, uint32_t n) {
 
 namespace {
 
-// per-process device context (the current device at first use)
+// the current device's context (made with that device current on first use)
 bool ctx(int &sms, uint32_t *&err) {
-  std::lock_guard<std::mutex> lk(g_state.mu);
-  if (g_state.device < 0) {
-    int dev;
-    if (cudaGetDevice(&dev) != cudaSuccess) return false;
-    int n;
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
-    uint32_t *e;
-    if (cudaMalloc(&e, sizeof(uint32_t)) != cudaSuccess) return false;
-    if (cudaMemset(e, 0, sizeof(uint32_t)) != cudaSuccess) return false;
-    g_state.device = dev; g_state.sms = n; g_state.err = e;
-  }
-  sms = g_state.sms; err = g_state.err;
+  DevCtx c{};
+  const bool ok = g_dev.get([](int &dev) { return cudaGetDevice(&dev) == cudaSuccess; },
+                            [](int dev, DevCtx &v) {
+                              int n;
+                              if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+                                return false;
+                              uint32_t *e;
+                              if (cudaMalloc(&e, sizeof(uint32_t)) != cudaSuccess) return false;
+                              if (cudaMemset(e, 0, sizeof(uint32_t)) != cudaSuccess) { cudaFree(e); return false; }
+                              v.sms = n; v.err = e;
+                              return true;
+                            },
+                            c);
+  if (!ok) return false;
+  sms = c.sms; err = c.err;
   return true;
 }
 

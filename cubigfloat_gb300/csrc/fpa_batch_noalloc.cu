@@ -1,23 +1,25 @@
 // fpa_batch_noalloc.cu -- a batched run that allocates no memory.
 //
-// fpa_batch_run_noalloc is for callers that are not allowed to allocate GPU memory at the
-// point where they compute: code that runs while a stream is being captured into a CUDA
-// graph, code in a serving or real-time loop that must never wait on the allocator, and
-// host applications that give this library a fixed memory footprint up front and treat any
-// later allocation as a failure.  They pass inputs and outputs in memory they already own;
-// the batch's own working memory (descriptors, schedule, task counters and the error word)
-// lives in one fixed array in device memory, sized for FPA_NOALLOC_MAX_OPS operations.
+// fpa_batch_run_noalloc is for callers that must not allocate GPU memory at the point where
+// they compute: a serving loop whose latency budget cannot absorb cudaMalloc / cudaFree
+// (which may synchronize the device and wait on unrelated work), and host applications
+// that give all device memory to their own allocator up front and treat any later
+// allocation by a library as a failure.  They pass inputs and outputs in memory they
+// already own; the batch's own working memory (descriptors, schedule, task counters and the
+// error word) lives in one fixed array in device memory, sized for FPA_NOALLOC_MAX_OPS
+// operations.  Nothing here calls cudaMalloc, cudaFree or an allocating library routine.
 //
 // The array is a file-scope __device__ variable, so every GPU that loads the library keeps
 // it (about 200 KB) until the process exits.  Host code cannot use the variable's name as a
 // device address; the first call on each device looks the address up with
-// cudaGetSymbolAddress while that device is current, and later calls reuse it.  That first
-// call therefore has to happen outside any stream capture.  Every call shares the array and
-// it keeps the last call's contents; the task counters and the error word are cleared by
-// each call before its kernels run, and two calls whose work overlaps on the GPU race on
-// the array, so calls must be ordered (one stream, or an event between streams).
-// Planning uses fixed host arrays under a lock and the class kernels run one after the
-// other on the caller's stream.
+// cudaGetSymbolAddress while that device is current, and later calls reuse it, so that
+// first call should come before any stream capture, and a device reset (which would give the
+// variable a new address) is not supported.  Every call shares the array and it keeps the
+// last call's contents; the task counters and the error word are cleared by each call
+// before its kernels run, and two calls whose work overlaps on the GPU race on the array,
+// so calls must be ordered (one stream, or an event between streams).  Planning uses fixed
+// host arrays under a lock and the class kernels run one after the other on the caller's
+// stream.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <mutex>
@@ -29,7 +31,7 @@
 namespace {
 
 constexpr uint32_t kMaxOps = FPA_NOALLOC_MAX_OPS;
-constexpr uint32_t kMaxTasks = kMaxOps + 64;       // tasks <= ops + number of (config, op) buckets
+constexpr uint32_t kMaxTasks = kMaxOps;            // every task holds at least one operation
 constexpr size_t kOffDescs = 0;
 constexpr size_t kOffOrder = kOffDescs + (size_t)kMaxOps * sizeof(fpa_batch_desc);
 constexpr size_t kOffTasks = kOffOrder + (size_t)kMaxOps * 4;

@@ -32,15 +32,28 @@ __constant__ uint8_t c_neg[9] = {0, 1, 2, 4, 3, 6, 5, 7, 8};
 
 __device__ __forceinline__ uint32_t classify(uint32_t e) { return e <= 8u ? e : (e & 1u); }
 
-// Writes an unsigned 64-bit magnitude (nonzero) as a normalized number; truncates when
-// the precision is 32 bits.  Returns the exponent word for a positive value.
+// Writes an unsigned 64-bit magnitude (nonzero) times 2^extra_exp as a normalized number.
+// Two or more limbs hold it exactly.  At one limb (precision 32) the 32 bits below the limb
+// are rounded to nearest, ties to even, as mpfr_set_ui / mpfr_set_d do with MPFR_RNDN (the
+// reference's precisions, 1024 bits and up, never round here).  Returns the exponent word
+// for a positive value.
 __device__ uint32_t put_u64(uint32_t *r, uint32_t n, uint64_t v, int extra_exp) {
   int s = __clzll((long long)v);
   v <<= s;
-  for (uint32_t i = 0; i < n; i++) r[i] = 0;
-  r[n - 1] = (uint32_t)(v >> 32);
-  if (n >= 2) r[n - 2] = (uint32_t)v;
   long long e = 64 - s + extra_exp;
+  uint32_t hi = (uint32_t)(v >> 32);
+  const uint32_t lo = (uint32_t)v;
+  if (n == 1) {
+    if ((lo >> 31) && ((lo << 1) | (hi & 1u))) {       // above one half, or a tie on an odd limb
+      hi++;
+      if (hi == 0) { hi = 0x80000000u; e++; }         // 0.11..1 + ulp = 1.0
+    }
+    r[0] = hi;
+  } else {
+    for (uint32_t i = 0; i + 2 < n; i++) r[i] = 0;
+    r[n - 1] = hi;
+    r[n - 2] = lo;
+  }
   return (uint32_t)(2 * ((long long)BIAS + e));
 }
 

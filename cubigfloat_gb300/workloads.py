@@ -242,6 +242,36 @@ def served_job(rng, precision=None, size=None, max_ops=4096):
     return precision, ops, modes, ae, al.reshape(-1), be, bl.reshape(-1)
 
 
+def reference_style_bulk(rng, count, n, signs=True, shift_frac=5 / 8):
+    """The reference test generator's pattern (tests.c:173-181, 815-830) for large counts,
+    vectorised: limbs drawn from {0, 1, 0x7FFFFFFF, 0x80000000, 0xFFFFFFFF}, normalised
+    (an all-zero draw becomes 2^(p-1)), exponent offset drawn as the difference of two
+    uniform values below 5/8 of the precision, random sign when `signs`."""
+    vals = np.array([0, 1, 0x7FFFFFFF, 0x80000000, 0xFFFFFFFF], dtype=np.uint32)
+    raw = vals[rng.integers(0, 5, size=(count, n))]
+    p = 32 * n
+    nz = raw != 0
+    top = np.where(nz.any(axis=1), n - 1 - np.argmax(nz[:, ::-1], axis=1), -1)      # highest nonzero limb
+    raw[top < 0, n - 1] = 0x80000000
+    top[top < 0] = n - 1
+    tl = raw[np.arange(count), top].astype(np.uint64)
+    L = 32 * top + np.floor(np.log2(np.maximum(tl, 1).astype(np.float64))).astype(np.int64) + 1
+    sh = p - L                                           # left shift that sets the top bit
+    q, r = sh // 32, (sh % 32).astype(np.uint64)
+    idx = np.arange(n)[None, :] - q[:, None]             # source limb of each destination limb
+    lo_idx = idx - 1
+    get = lambda ix: np.where((ix >= 0) & (ix < n), raw[np.arange(count)[:, None], np.clip(ix, 0, n - 1)], 0)
+    hi = get(idx).astype(np.uint64)
+    lo = get(lo_idx).astype(np.uint64)
+    rr = r[:, None]
+    limbs = ((hi << rr) | np.where(rr > 0, lo >> (np.uint64(32) - rr), np.uint64(0))) & np.uint64(0xFFFFFFFF)
+    limbs = limbs.astype(np.uint32)
+    span = max(1, int(p * shift_frac))
+    e = L - p + rng.integers(0, span, size=count) - rng.integers(0, span, size=count)
+    s = rng.integers(0, 2, size=count) if signs else np.zeros(count, dtype=np.int64)
+    return exp_word(e, s), limbs
+
+
 def poisson_arrivals(rng, njobs, rate_per_s):
     """Arrival times (seconds from start) of a Poisson process."""
     return np.cumsum(rng.exponential(1.0 / rate_per_s, size=njobs))

@@ -15,8 +15,13 @@
  *     1024..8192 in steps of 1024, fpa_management.h:2-3);
  *   - errors from the CUDA runtime are returned as fpa_device_error instead of printing
  *     and exiting the process (fpa.cu:34);
- *   - results are correctly rounded in all five modes (see INTEGRATION.md for the
- *     reference behaviours this corrects).
+ *   - results are correctly rounded in all five modes, also where the reference's kernels
+ *     are not: exact ties after mul's one-bit normalisation (fpa_warp_mul.h:115-121), a
+ *     mul result whose high half is all ones (:99-105), 0 - b (fpa_warp_add_sub.h:357-379)
+ *     and sqrt rounding up into the next binade (fpa_warp_sqrt.h:238-242);
+ *   - fpa_set stores the rounded limbs (the reference's kernel never stores them,
+ *     fpa_warp_set.h:134-199), and at precision 32 the conversions round a wider integer or
+ *     double mantissa to nearest, ties to even.
  */
 #ifndef FPA_H
 #define FPA_H

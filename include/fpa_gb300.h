@@ -34,8 +34,10 @@ fpa_result fpa_op_async(fpa_op op, fpa_t r, fpa_t a, fpa_t b, fpa_rounding_mode 
 fpa_result fpa_copy_array_to_device_async(fpa_t fpa, const uint32_t *exps, const uint32_t *limbs, void *stream);
 fpa_result fpa_copy_array_to_host_async(fpa_t fpa, uint32_t *exps, uint32_t *limbs, void *stream);
 
-/* Error bits raised by kernels since the previous call, then cleared (synchronizes the
- * device): 1 = a division's correction loop hit its bound, 2 = same for sqrt. */
+/* Error bits raised by kernels on the current device since the previous call, then
+ * cleared (synchronizes the device): 1 = a division's correction loop hit its bound, 2 =
+ * same for sqrt.  The library keeps one such word (and its SM count) per device, made on
+ * the first call that finds the device current. */
 uint32_t fpa_gb300_device_errors(void);
 
 /* r = RND(a*b + c) with a single rounding (no counterpart in the reference, whose API has
@@ -142,17 +144,20 @@ fpa_result fpa_server_destroy(fpa_server_t server);
 
 /* Batched run without any memory allocation.  No counterpart in the reference.
  *
- * For callers that may not allocate GPU memory where they compute (while a stream is being
- * captured into a graph, inside a serving loop that must never wait on the allocator, or
- * in a host application that fixes this library's memory footprint up front): inputs and
- * outputs are the caller's device arrays, and the batch's working memory is one fixed
- * device array sized for FPA_NOALLOC_MAX_OPS operations, which every GPU that loads the
- * library holds until the process exits.  More operations than that: fpa_invalid_counts.
- * The first call on each device looks up that array's address and must come before any
- * stream capture.  All calls share the array (it keeps the last call's contents; each call
- * clears its counters and error word itself), so calls must not overlap on the GPU.  The
- * host descriptors are read during the call.  Error bits of the bounded correction loops
- * are read with fpa_batch_noalloc_errors (which synchronizes `stream`). */
+ * For callers that must not allocate GPU memory at the point where they compute: a serving
+ * loop whose latency budget cannot absorb cudaMalloc / cudaFree (which may synchronize the
+ * device and wait on other work), and host applications that hand all device memory to
+ * their own allocator up front and treat any later allocation by a library as a failure.
+ * Inputs and outputs are the caller's device arrays.  The batch's working memory is one
+ * fixed device array sized for FPA_NOALLOC_MAX_OPS operations, which every GPU that loads
+ * the library holds until the process exits; more operations than that return
+ * fpa_invalid_counts.  The first call on each device looks up that array's device address
+ * (with that device current) and should come before any stream capture.  All calls share
+ * the array and it keeps the last call's contents: each call clears its task counters and
+ * error word itself, and calls that overlap on the GPU race on the array, so order them
+ * (one stream, or an event between streams).  A device reset is not supported (the looked-
+ * up address is kept).  Error bits of the bounded correction loops are read with
+ * fpa_batch_noalloc_errors (which synchronizes `stream`). */
 #define FPA_NOALLOC_MAX_OPS 4096
 fpa_result fpa_batch_run_noalloc(const fpa_batch_desc *descs, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs,
                                  const uint32_t *a_exps, const uint32_t *a_limbs,
@@ -183,6 +188,10 @@ uint32_t fpa_gb300_get_karatsuba_limbs(void);
 /* Measured integer multiply-add throughput of the current GPU (mad.lo.u32 and mad.hi.u32
  * per second over all SMs): the roofline denominator for the multiply-bound operations. */
 fpa_result fpa_gb300_measure_imad_peak(double *mad_lo_per_s, double *mad_hi_per_s);
+/* Measured limb-product throughput of the current GPU: 32x32-bit products accumulated into
+ * 96-bit columns per second over all SMs, issued as the product kernels issue them
+ * (mad.lo.cc, madc.hi.cc, addc per product) -- the roofline denominator for mul/div/sqrt. */
+fpa_result fpa_gb300_measure_product_peak(double *products_per_s);
 
 const char *fpa_gb300_version(void);
 

@@ -43,6 +43,17 @@ def lib():
         L.oracle_mixed.argtypes = [u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32]
         L.oracle_fma_batch.restype = i32
         L.oracle_fma_batch.argtypes = [u32, i32, u32, vp, vp, vp, vp, vp, vp, vp, vp]
+        for name in ("oracle_set_ui", "oracle_set_si", "oracle_set_float", "oracle_set_double"):
+            getattr(L, name).restype = i32
+            getattr(L, name).argtypes = [u32, u32, vp, vp, vp]
+        L.oracle_set_prec.restype = i32
+        L.oracle_set_prec.argtypes = [u32, u32, i32, u32, vp, vp, vp, vp]
+        L.oracle_sgn.restype = i32
+        L.oracle_sgn.argtypes = [u32, vp, vp]
+        L.oracle_cmp.restype = i32
+        L.oracle_cmp.argtypes = [u32, u32, vp, vp, vp, vp, vp]
+        L.oracle_neg.restype = i32
+        L.oracle_neg.argtypes = [u32, u32, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -99,16 +110,77 @@ def run_mixed(ops, ns, modes, a_exps, a_limbs, a_off, b_exps, b_limbs, b_off, r_
     return r_exps, r_limbs
 
 
+# ---- conversions, sign, compare, negation ------------------------------------------
+_SET_KIND = {"ui": ("oracle_set_ui", np.uint64), "si": ("oracle_set_si", np.int64),
+             "float": ("oracle_set_float", np.float32), "double": ("oracle_set_double", np.float64)}
+
+
+def set_values(kind, n, values):
+    """fpa_set_ui / si / float / double of `values` at n limbs; returns (r_exps, r_limbs).
+    Class results leave their limbs zero."""
+    name, dt = _SET_KIND[kind]
+    v = np.ascontiguousarray(values, dtype=dt)
+    if kind in ("float", "double"):
+        v = v.view(np.uint32 if kind == "float" else np.uint64)
+    count = v.size
+    r_exps = np.zeros(count, dtype=np.uint32)
+    r_limbs = np.zeros((count, n), dtype=np.uint32)
+    if getattr(lib(), name)(n, count, _p(r_exps), _p(r_limbs), _p(v)) != 0:
+        raise ValueError(f"{name} failed")
+    return r_exps, r_limbs
+
+
+def set_prec(nr, nx, mode, x_exps, x_limbs):
+    """fpa_set: numbers of nx limbs rounded to nr limbs in `mode`."""
+    x_exps = np.ascontiguousarray(x_exps, dtype=np.uint32)
+    x_limbs = np.ascontiguousarray(x_limbs, dtype=np.uint32).reshape(-1, nx)
+    count = x_exps.size
+    r_exps = np.zeros(count, dtype=np.uint32)
+    r_limbs = np.zeros((count, nr), dtype=np.uint32)
+    if lib().oracle_set_prec(nr, nx, mode, count, _p(r_exps), _p(r_limbs), _p(x_exps), _p(x_limbs)) != 0:
+        raise ValueError("oracle_set_prec failed")
+    return r_exps, r_limbs
+
+
+def sgn(x_exps):
+    x_exps = np.ascontiguousarray(x_exps, dtype=np.uint32)
+    r = np.zeros(x_exps.size, dtype=np.int32)
+    lib().oracle_sgn(x_exps.size, _p(r), _p(x_exps))
+    return r
+
+
+def cmp(n, a_exps, a_limbs, b_exps, b_limbs):
+    arr = [np.ascontiguousarray(x, dtype=np.uint32) for x in (a_exps, a_limbs, b_exps, b_limbs)]
+    r = np.zeros(arr[0].size, dtype=np.int32)
+    if lib().oracle_cmp(n, arr[0].size, _p(r), *[_p(x) for x in arr]) != 0:
+        raise ValueError("oracle_cmp failed")
+    return r
+
+
+def neg(n, a_exps, a_limbs):
+    a_exps = np.ascontiguousarray(a_exps, dtype=np.uint32)
+    a_limbs = np.ascontiguousarray(a_limbs, dtype=np.uint32).reshape(-1, n)
+    r_exps = np.zeros(a_exps.size, dtype=np.uint32)
+    r_limbs = np.zeros((a_exps.size, n), dtype=np.uint32)
+    if lib().oracle_neg(n, a_exps.size, _p(r_exps), _p(r_limbs), _p(a_exps), _p(a_limbs)) != 0:
+        raise ValueError("oracle_neg failed")
+    return r_exps, r_limbs
+
+
 # ---- the reference's own kernels (compiled from its sources, test use only) ----------
 REF_DIR = os.path.join(HERE, "_ref")
 REF_CUBIN = os.path.join(REF_DIR, "ref_fpa.cubin")
 
 
-def build_ref(reference_root=os.environ.get("FPA_REFERENCE_ROOT", "/root/reference")):
+def build_ref(reference_root=None):
     """Compile the reference's device code (its single translation unit fpa.cu) for sm_103a
     into oracle/_ref/ref_fpa.cubin.  Runs only where the reference sources are present; the
     cubin is loaded by tests through the CUDA driver API to compare against the reference's
-    own GPU output.  Returns the cubin path or None."""
+    own GPU output.  The sources are looked for in $FPA_REFERENCE_ROOT, else in a directory
+    named `reference` beside the repository.  Returns the cubin path or None."""
+    if reference_root is None:
+        reference_root = os.environ.get("FPA_REFERENCE_ROOT",
+                                        os.path.join(os.path.dirname(HERE), os.pardir, "reference"))
     src = os.path.join(reference_root, "fpa.cu")
     if not os.path.exists(src):
         return REF_CUBIN if os.path.exists(REF_CUBIN) else None

@@ -510,6 +510,147 @@ int oracle_op(int op, uint32_t n, int mode, uint32_t *r_exp, uint32_t *r_limbs,
   return -1;
 }
 
+/* ---- conversions, sign, compare, negation (the non-arithmetic fpa.h entry points) ----
+ *
+ * fpa_set_ui/si/float/double (fpa_warp_set.h:1-132, dispatch fpa_dispatch.h:8-86): the
+ * value is stored exactly whenever it fits the precision, which is always the case at the
+ * reference's precisions (>= 1024 bits).  The precision-32 numbers of this library hold
+ * only 32 bits, so a wider integer or double mantissa is rounded to nearest, ties to even
+ * (what mpfr_set_ui / mpfr_set_d give with MPFR_RNDN).  Zero (either sign) is the ZERO
+ * class, every NaN (quiet or signalling, any payload) the NAN class, infinities the INF
+ * classes (fpa_warp_set.h:89-96). */
+static void put_int(uint32_t n, uint64_t mag, int sign, int64_t e0, uint32_t *r_exp, uint32_t *r_limbs) {
+  if (mag == 0) { *r_exp = C_ZERO; return; }
+  uint32_t X[2] = { (uint32_t)mag, (uint32_t)(mag >> 32) };
+  uint32_t *M = (uint32_t *)calloc(n, 4);
+  int64_t e = round_pack(n, 3, sign, X, 2, e0, 0, M);
+  memcpy(r_limbs, M, 4 * (size_t)n);
+  *r_exp = encode(e, sign);
+  free(M);
+}
+
+int oracle_set_ui(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const uint64_t *vals) {
+  if (n == 0 || n > 4096) return -1;
+  for (uint32_t i = 0; i < count; i++) put_int(n, vals[i], 0, 0, r_exps + i, r_limbs + (size_t)i * n);
+  return 0;
+}
+
+/* fpa_warp_set.h:34-41 (INT64_MIN has magnitude 2^63) */
+int oracle_set_si(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const int64_t *vals) {
+  if (n == 0 || n > 4096) return -1;
+  for (uint32_t i = 0; i < count; i++) {
+    const int neg = vals[i] < 0;
+    const uint64_t mag = neg ? (uint64_t)0 - (uint64_t)vals[i] : (uint64_t)vals[i];
+    put_int(n, mag, neg, 0, r_exps + i, r_limbs + (size_t)i * n);
+  }
+  return 0;
+}
+
+/* IEEE binary32 / binary64 from their bit patterns: (-1)^s * m * 2^q with integer m
+ * (fpa_warp_set.h:74-132 uses frexp/ldexp for the same decomposition). */
+static void put_ieee(uint32_t n, uint64_t bits, int is_double, uint32_t *r_exp, uint32_t *r_limbs) {
+  const int mbits = is_double ? 52 : 23, ebits = is_double ? 11 : 8;
+  const int sign = (int)((bits >> (mbits + ebits)) & 1u);
+  const int ef = (int)((bits >> mbits) & ((1u << ebits) - 1u));
+  uint64_t m = bits & ((1ull << mbits) - 1u);
+  const int bias = (1 << (ebits - 1)) - 1;
+  if (ef == (1 << ebits) - 1) { *r_exp = m ? C_NAN : (sign ? C_NEG_INF : C_POS_INF); return; }
+  int64_t q;
+  if (ef == 0) q = 1 - bias - mbits;
+  else { m |= 1ull << mbits; q = ef - bias - mbits; }
+  put_int(n, m, sign, q, r_exp, r_limbs);
+}
+
+int oracle_set_float(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *bits) {
+  if (n == 0 || n > 4096) return -1;
+  for (uint32_t i = 0; i < count; i++) put_ieee(n, bits[i], 0, r_exps + i, r_limbs + (size_t)i * n);
+  return 0;
+}
+
+int oracle_set_double(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const uint64_t *bits) {
+  if (n == 0 || n > 4096) return -1;
+  for (uint32_t i = 0; i < count; i++) put_ieee(n, bits[i], 1, r_exps + i, r_limbs + (size_t)i * n);
+  return 0;
+}
+
+/* fpa_set: change of precision with rounding in `mode` (fpa_warp_set.h:134-199 decides the
+ * rounding but never stores the limbs; here the rounded value is stored).  Class operands
+ * are copied; rounding up past the largest exponent gives +/-INF (the mul limit,
+ * fpa_warp_mul.h:124-128). */
+int oracle_set_prec(uint32_t nr, uint32_t nx, int mode, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs,
+                    const uint32_t *x_exps, const uint32_t *x_limbs) {
+  if (nr == 0 || nr > 4096 || nx == 0 || nx > 4096 || mode < 0 || mode > 4) return -1;
+  uint32_t *M = (uint32_t *)calloc(nr, 4);
+  for (uint32_t i = 0; i < count; i++) {
+    const uint32_t xe = x_exps[i];
+    if (classify(xe) > C_NEG_VALUE) { r_exps[i] = xe; continue; }
+    const int sign = (int)(xe & 1u);
+    const int64_t ex = (int64_t)(xe >> 1) - BIAS;
+    const int64_t e = round_pack(nr, mode, sign, x_limbs + (size_t)i * nx, (int)nx, ex - 32LL * nx, 0, M);
+    if (BIAS + e > 0x7FFFFFFFLL) { r_exps[i] = C_POS_INF - sign; continue; }
+    r_exps[i] = encode(e, sign);
+    memcpy(r_limbs + (size_t)i * nr, M, 4 * (size_t)nr);
+  }
+  free(M);
+  return 0;
+}
+
+/* fpa_threaded.h:1-11 (sgn) and :13-24 (cmp): class tables; a NaN operand (the tables'
+ * error entry) gives 0, as in fpa_threaded.h:34-37.  CMP_V = compare the values. */
+enum { CMP_V = 25, CMP_E = 26 };
+static const int8_t sgn_table[9] = { +1, -1, 0, -1, +1, -1, +1, CMP_E, CMP_E };
+static const int8_t cmp_table[81] = {
+  CMP_V, +1,    +1,    +1,    +1,    +1,    -1,    CMP_E, CMP_E,
+  -1,    CMP_V, -1,    -1,    -1,    +1,    -1,    CMP_E, CMP_E,
+  -1,    +1,    0,     +1,    -1,    +1,    -1,    CMP_E, CMP_E,
+  -1,    +1,    -1,    CMP_E, -1,    +1,    -1,    CMP_E, CMP_E,
+  -1,    +1,    +1,    +1,    CMP_E, +1,    -1,    CMP_E, CMP_E,
+  -1,    -1,    -1,    -1,    -1,    CMP_E, -1,    CMP_E, CMP_E,
+  +1,    +1,    +1,    +1,    +1,    +1,    CMP_E, CMP_E, CMP_E,
+  CMP_E, CMP_E, CMP_E, CMP_E, CMP_E, CMP_E, CMP_E, CMP_E, CMP_E,
+  CMP_E, CMP_E, CMP_E, CMP_E, CMP_E, CMP_E, CMP_E, CMP_E, CMP_E,
+};
+/* fpa_warp_add_sub.h:3-13: the class of -x for each class of x */
+static const uint8_t neg_table[9] = { 0, 1, C_ZERO, C_POS_TINY, C_NEG_TINY, C_POS_INF, C_NEG_INF, C_NAN, C_SNAN };
+
+int oracle_sgn(uint32_t count, int32_t *r, const uint32_t *x_exps) {
+  for (uint32_t i = 0; i < count; i++) {
+    const int a = sgn_table[classify(x_exps[i])];
+    r[i] = a == CMP_E ? 0 : a;
+  }
+  return 0;
+}
+
+/* values of one sign: the exponent words order them, then the limbs from the top
+ * (fpa_threaded.h:52-89) */
+int oracle_cmp(uint32_t n, uint32_t count, int32_t *r, const uint32_t *a_exps, const uint32_t *a_limbs,
+               const uint32_t *b_exps, const uint32_t *b_limbs) {
+  if (n == 0 || n > 4096) return -1;
+  for (uint32_t i = 0; i < count; i++) {
+    const uint32_t ae = a_exps[i], be = b_exps[i];
+    const int act = cmp_table[classify(ae) * 9 + classify(be)];
+    if (act == CMP_E) { r[i] = 0; continue; }
+    if (act != CMP_V) { r[i] = act; continue; }
+    const int sgn = (ae & 1u) ? -1 : 1;
+    int c = ae > be ? 1 : (ae < be ? -1 : cmp_n(a_limbs + (size_t)i * n, b_limbs + (size_t)i * n, (int)n));
+    r[i] = sgn * c;
+  }
+  return 0;
+}
+
+/* fpa_warp_neg (fpa_warp_add_sub.h:284-308): values flip the sign bit and copy the limbs */
+int oracle_neg(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *a_exps,
+               const uint32_t *a_limbs) {
+  if (n == 0 || n > 4096) return -1;
+  for (uint32_t i = 0; i < count; i++) {
+    const uint32_t ae = a_exps[i];
+    if (ae <= C_SNAN) { r_exps[i] = neg_table[ae]; continue; }
+    r_exps[i] = ae ^ 1u;
+    memcpy(r_limbs + (size_t)i * n, a_limbs + (size_t)i * n, 4 * (size_t)n);
+  }
+  return 0;
+}
+
 /* ---- threaded batch runners ------------------------------------------------ */
 
 typedef struct {

@@ -56,6 +56,21 @@ int oracle_mixed(uint32_t count, const uint8_t *ops, const uint16_t *limbs_n, co
                  const uint32_t *b_exps, const uint32_t *b_limbs, const uint64_t *b_off,
                  int threads);
 
+/* Conversions into the format (fpa_set_ui/si/float/double; floats and doubles given as
+ * their IEEE bit patterns), precision change (fpa_set, nx -> nr limbs, rounded in `mode`),
+ * sign, compare and negation, each over `count` instances.  Return 0, or -1 for bad sizes. */
+int oracle_set_ui(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const uint64_t *vals);
+int oracle_set_si(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const int64_t *vals);
+int oracle_set_float(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *bits);
+int oracle_set_double(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const uint64_t *bits);
+int oracle_set_prec(uint32_t nr, uint32_t nx, int mode, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs,
+                    const uint32_t *x_exps, const uint32_t *x_limbs);
+int oracle_sgn(uint32_t count, int32_t *r, const uint32_t *x_exps);
+int oracle_cmp(uint32_t n, uint32_t count, int32_t *r, const uint32_t *a_exps, const uint32_t *a_limbs,
+               const uint32_t *b_exps, const uint32_t *b_limbs);
+int oracle_neg(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *a_exps,
+               const uint32_t *a_limbs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,16 @@ def lib():
             L.gold_batch3.restype = i32
             L.gold_batch3.argtypes = [i32, u32, i32, u32, vp, vp, vp, vp, vp, vp, vp, vp]
             L.gold_version.restype = ctypes.c_char_p
+            L.gold_set.restype = i32
+            L.gold_set.argtypes = [i32, u32, u32, vp, vp, vp]
+            L.gold_set_prec.restype = i32
+            L.gold_set_prec.argtypes = [u32, u32, i32, u32, vp, vp, vp, vp]
+            L.gold_sgn.restype = i32
+            L.gold_sgn.argtypes = [u32, u32, vp, vp, vp]
+            L.gold_cmp.restype = i32
+            L.gold_cmp.argtypes = [u32, u32, vp, vp, vp, vp, vp]
+            L.gold_neg.restype = i32
+            L.gold_neg.argtypes = [u32, u32, vp, vp, vp, vp]
             _lib = L
         except Exception as e:  # libmpfr absent
             _err = e
@@ -83,4 +93,59 @@ def run_fma(n, mode, a_exps, a_limbs, b_exps, b_limbs, c_exps, c_limbs):
     bad = lib().gold_batch3(5, n, mode, count, _p(r_exps), _p(r_limbs), *[_p(x) for x in arr])
     if bad:
         raise ValueError(f"{bad} MPFR results were not finite")
+    return r_exps, r_limbs
+
+
+_SET_KIND = {"ui": (0, np.uint64), "si": (1, np.int64), "float": (2, np.float32), "double": (3, np.float64)}
+
+
+def set_values(kind, n, values):
+    """mpfr_set_ui / set_si / set_flt / set_d at precision 32n, round to nearest; class
+    results (zero, inf, NaN) as the fpa class codes with zero limbs."""
+    k, dt = _SET_KIND[kind]
+    v = np.ascontiguousarray(values, dtype=dt)
+    r_exps = np.zeros(v.size, dtype=np.uint32)
+    r_limbs = np.zeros((v.size, n), dtype=np.uint32)
+    bad = lib().gold_set(k, n, v.size, _p(r_exps), _p(r_limbs), _p(v))
+    if bad:
+        raise ValueError(f"{bad} conversions failed")
+    return r_exps, r_limbs
+
+
+def set_prec(nr, nx, mode, x_exps, x_limbs):
+    """mpfr_set from 32nx to 32nr bits in `mode` (inputs must be values)."""
+    x_exps = np.ascontiguousarray(x_exps, dtype=np.uint32)
+    x_limbs = np.ascontiguousarray(x_limbs, dtype=np.uint32).reshape(-1, nx)
+    r_exps = np.zeros(x_exps.size, dtype=np.uint32)
+    r_limbs = np.zeros((x_exps.size, nr), dtype=np.uint32)
+    bad = lib().gold_set_prec(nr, nx, mode, x_exps.size, _p(r_exps), _p(r_limbs), _p(x_exps), _p(x_limbs))
+    if bad:
+        raise ValueError(f"{bad} precision changes failed")
+    return r_exps, r_limbs
+
+
+def sgn(n, x_exps, x_limbs):
+    x_exps = np.ascontiguousarray(x_exps, dtype=np.uint32)
+    x_limbs = np.ascontiguousarray(x_limbs, dtype=np.uint32)
+    r = np.zeros(x_exps.size, dtype=np.int32)
+    if lib().gold_sgn(n, x_exps.size, _p(r), _p(x_exps), _p(x_limbs)):
+        raise ValueError("gold_sgn: input without an MPFR counterpart")
+    return r
+
+
+def cmp(n, a_exps, a_limbs, b_exps, b_limbs):
+    arr = [np.ascontiguousarray(x, dtype=np.uint32) for x in (a_exps, a_limbs, b_exps, b_limbs)]
+    r = np.zeros(arr[0].size, dtype=np.int32)
+    if lib().gold_cmp(n, arr[0].size, _p(r), *[_p(x) for x in arr]):
+        raise ValueError("gold_cmp: input without an MPFR counterpart")
+    return r
+
+
+def neg(n, a_exps, a_limbs):
+    a_exps = np.ascontiguousarray(a_exps, dtype=np.uint32)
+    a_limbs = np.ascontiguousarray(a_limbs, dtype=np.uint32).reshape(-1, n)
+    r_exps = np.zeros(a_exps.size, dtype=np.uint32)
+    r_limbs = np.zeros((a_exps.size, n), dtype=np.uint32)
+    if lib().gold_neg(n, a_exps.size, _p(r_exps), _p(r_limbs), _p(a_exps), _p(a_limbs)):
+        raise ValueError("gold_neg: input without an MPFR counterpart")
     return r_exps, r_limbs

@@ -5,6 +5,10 @@ Writes tests/golden/fixtures/<op>_n<limbs>.npz with the operands (a_*, b_*) and,
 rounding mode m = 0..4, the MPFR result (r_exps[m], r_limbs[m]).  Operand sets per file:
 uniform mantissas, the reference test generator's limb pattern (tests.c:173-181) and the
 near-halfway / near-exact constructions of the 4096-bit workload.
+
+Also writes tests/golden/conv/conv_mpfr.npz: mpfr_set_ui / set_si / set_flt / set_d
+(round to nearest), mpfr_set between precisions in all five modes, and mpfr_sgn /
+mpfr_cmp / mpfr_neg, on the seeded inputs of tests/conv_cases.py.
 """
 import os
 import sys
@@ -14,12 +18,16 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+import conv_cases as CC  # noqa: E402
 import gold  # noqa: E402
 from cubigfloat_gb300 import workloads as W  # noqa: E402
 
 OPS = ["add", "sub", "mul", "div", "sqrt"]
 SIZES = {1: 24, 8: 24, 32: 24, 33: 24, 64: 16, 128: 16, 160: 6}
 OUT = os.path.join(ROOT, "tests", "golden", "fixtures")
+CONV_OUT = os.path.join(ROOT, "tests", "golden", "conv", "conv_mpfr.npz")
+CONV_SIZES = (1, 2, 32, 128)
 
 
 def operands(op, n, count, seed):
@@ -69,7 +77,44 @@ def main():
                                 r_exps=np.stack(r_e), r_limbs=np.stack(r_l),
                                 mpfr_version=gold.version())
     print("wrote", len(os.listdir(OUT)), "fixtures to", OUT)
+    conversions()
+
+
+def conversions():
+    """MPFR results for the conversion, precision-change, sign, compare and negation cases."""
+    z = {"mpfr_version": gold.version()}
+    inputs = {"ui": CC.uint_values(1), "si": CC.int_values(2), "float": CC.float_bits(3).view(np.float32),
+              "double": CC.double_bits(4).view(np.float64)}
+    for kind, v in inputs.items():
+        z[f"set_{kind}_in"] = v
+        for n in CONV_SIZES:
+            e, l = gold.set_values(kind, n, v)
+            z[f"set_{kind}_n{n}_exps"], z[f"set_{kind}_n{n}_limbs"] = e, l
+    for nx, nr in CC.PREC_PAIRS:
+        if max(nx, nr) > 128:
+            continue
+        xe, xl = CC.prec_sources(10 * nx + nr, nx, nr)
+        z[f"prec_{nx}_{nr}_in_exps"], z[f"prec_{nx}_{nr}_in_limbs"] = xe, xl
+        outs = [gold.set_prec(nr, nx, m, xe, xl) for m in range(5)]
+        z[f"prec_{nx}_{nr}_exps"] = np.stack([o[0] for o in outs])
+        z[f"prec_{nx}_{nr}_limbs"] = np.stack([o[1] for o in outs])
+    for n in CONV_SIZES:
+        xe, xl = CC.numbers(50 + n, n, classes=CC.MPFR_CLASSES)
+        z[f"num_n{n}_exps"], z[f"num_n{n}_limbs"] = xe, xl
+        z[f"sgn_n{n}"] = gold.sgn(n, xe, xl)
+        ne, nl = gold.neg(n, xe, xl)
+        z[f"neg_n{n}_exps"], z[f"neg_n{n}_limbs"] = ne, nl
+        ae, al, be, bl = CC.compare_pairs(60 + n, n, classes=CC.MPFR_CLASSES)
+        z[f"cmp_n{n}_a_exps"], z[f"cmp_n{n}_a_limbs"] = ae, al
+        z[f"cmp_n{n}_b_exps"], z[f"cmp_n{n}_b_limbs"] = be, bl
+        z[f"cmp_n{n}"] = gold.cmp(n, ae, al, be, bl)
+    os.makedirs(os.path.dirname(CONV_OUT), exist_ok=True)
+    np.savez_compressed(CONV_OUT, **z)
+    print("wrote", CONV_OUT)
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--conversions"]:
+        conversions()
+    else:
+        main()

@@ -36,6 +36,18 @@ int mpfr_prec_round(mpfr_s *, mpfr_prec_t, int);
 int mpfr_zero_p(const mpfr_s *);
 int mpfr_nan_p(const mpfr_s *);
 int mpfr_inf_p(const mpfr_s *);
+int mpfr_set_ui(mpfr_s *, unsigned long, int);
+int mpfr_set_si(mpfr_s *, long, int);
+int mpfr_set_d(mpfr_s *, double, int);
+int mpfr_set_flt(mpfr_s *, float, int);
+int mpfr_set(mpfr_s *, const mpfr_s *, int);
+int mpfr_sgn(const mpfr_s *);
+int mpfr_cmp(const mpfr_s *, const mpfr_s *);
+int mpfr_neg(mpfr_s *, const mpfr_s *, int);
+int mpfr_signbit(const mpfr_s *);
+void mpfr_set_nan(mpfr_s *);
+void mpfr_set_inf(mpfr_s *, int);
+void mpfr_set_zero(mpfr_s *, int);
 const char *mpfr_get_version(void);
 void __gmpz_init(mpz_s *);
 void __gmpz_clear(mpz_s *);
@@ -138,4 +150,124 @@ int gold_batch(int op, uint32_t n, int mode, uint32_t count,
                const uint32_t *a_exps, const uint32_t *a_limbs,
                const uint32_t *b_exps, const uint32_t *b_limbs) {
   return gold_batch3(op, n, mode, count, r_exps, r_limbs, a_exps, a_limbs, b_exps, b_limbs, NULL, NULL);
+}
+
+
+/* ---- conversions, precision change, sign, compare, negation ------------------------ */
+
+/* like from_mpfr, with MPFR's special values mapped to the fpa classes: NaN -> NAN (7),
+ * -inf / +inf -> NEG_INF (5) / POS_INF (6), zero of either sign -> ZERO (2) */
+static int from_mpfr_any(uint32_t *exp, uint32_t *limbs, uint32_t n, const mpfr_s *x) {
+  if (mpfr_nan_p(x)) { *exp = 7; return 0; }
+  if (mpfr_inf_p(x)) { *exp = mpfr_signbit(x) ? 5 : 6; return 0; }
+  return from_mpfr(exp, limbs, n, x);
+}
+
+/* fpa number -> mpfr, with the classes MPFR can represent (ZERO, INF, NAN); returns -1 for
+ * the TINY classes and SNAN, which have no MPFR counterpart */
+static int to_mpfr_any(mpfr_s *x, uint32_t exp, const uint32_t *limbs, uint32_t n) {
+  if (exp > 8) { to_mpfr(x, exp, limbs, n); return 0; }
+  switch (exp) {
+    case 2: mpfr_set_zero(x, 1); return 0;
+    case 5: mpfr_set_inf(x, -1); return 0;
+    case 6: mpfr_set_inf(x, 1); return 0;
+    case 7: mpfr_set_nan(x); return 0;
+  }
+  return -1;
+}
+
+/* kind: 0 = mpfr_set_ui (uint64), 1 = mpfr_set_si (int64), 2 = mpfr_set_flt (float bits),
+ * 3 = mpfr_set_d (double bits); precision 32n, round to nearest (ties to even). */
+int gold_set(int kind, uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const void *vals) {
+  mpfr_s r;
+  mpfr_init2(&r, 32L * n);
+  int bad = 0;
+  for (uint32_t i = 0; i < count; i++) {
+    switch (kind) {
+      case 0: mpfr_set_ui(&r, (unsigned long)((const uint64_t *)vals)[i], RNDN); break;
+      case 1: mpfr_set_si(&r, (long)((const int64_t *)vals)[i], RNDN); break;
+      case 2: mpfr_set_flt(&r, ((const float *)vals)[i], RNDN); break;
+      default: mpfr_set_d(&r, ((const double *)vals)[i], RNDN); break;
+    }
+    if (from_mpfr_any(r_exps + i, r_limbs + (size_t)i * n, n, &r) != 0) bad++;
+  }
+  mpfr_clear(&r);
+  return bad;
+}
+
+/* mpfr_set from precision 32nx to 32nr in `mode` (fpa_rounding_mode; ties-away as in
+ * gold_batch3).  Inputs must be values. */
+int gold_set_prec(uint32_t nr, uint32_t nx, int mode, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs,
+                  const uint32_t *x_exps, const uint32_t *x_limbs) {
+  static const int map[4] = { RNDZ, RNDU, RNDD, RNDN };
+  mpfr_s x, r;
+  const mpfr_prec_t p = 32L * nr;
+  mpfr_init2(&x, 32L * nx); mpfr_init2(&r, p);
+  int bad = 0;
+  for (uint32_t i = 0; i < count; i++) {
+    to_mpfr(&x, x_exps[i], x_limbs + (size_t)i * nx, nx);
+    if (mode == 4) {
+      mpfr_set_prec(&r, p + 1);
+      mpfr_set(&r, &x, RNDZ);
+      mpz_s z; __gmpz_init(&z);
+      mpfr_get_z_2exp(&z, &r);
+      int neg = z.size < 0; if (neg) z.size = -z.size;
+      uint32_t *tmp = (uint32_t *)calloc(nr + 3, 4); size_t w = 0;
+      __gmpz_export(tmp, &w, -1, 4, 0, 0, &z);
+      const uint32_t low = tmp[0] & 1u;
+      free(tmp);
+      __gmpz_clear(&z);
+      mpfr_prec_round(&r, p, low ? RNDA : RNDZ);
+    } else {
+      mpfr_set_prec(&r, p);
+      mpfr_set(&r, &x, map[mode]);
+    }
+    if (from_mpfr_any(r_exps + i, r_limbs + (size_t)i * nr, nr, &r) != 0) bad++;
+  }
+  mpfr_clear(&x); mpfr_clear(&r);
+  return bad;
+}
+
+/* mpfr_sgn, mpfr_cmp (NaN -> 0) and mpfr_neg on fpa numbers that are values or the
+ * ZERO / INF / NAN classes; returns the number of inputs MPFR cannot represent. */
+int gold_sgn(uint32_t n, uint32_t count, int32_t *r, const uint32_t *x_exps, const uint32_t *x_limbs) {
+  mpfr_s x;
+  mpfr_init2(&x, 32L * n);
+  int bad = 0;
+  for (uint32_t i = 0; i < count; i++) {
+    if (to_mpfr_any(&x, x_exps[i], x_limbs + (size_t)i * n, n) != 0) { bad++; continue; }
+    r[i] = mpfr_nan_p(&x) ? 0 : mpfr_sgn(&x);
+    r[i] = r[i] > 0 ? 1 : (r[i] < 0 ? -1 : 0);
+  }
+  mpfr_clear(&x);
+  return bad;
+}
+
+int gold_cmp(uint32_t n, uint32_t count, int32_t *r, const uint32_t *a_exps, const uint32_t *a_limbs,
+             const uint32_t *b_exps, const uint32_t *b_limbs) {
+  mpfr_s a, b;
+  mpfr_init2(&a, 32L * n); mpfr_init2(&b, 32L * n);
+  int bad = 0;
+  for (uint32_t i = 0; i < count; i++) {
+    if (to_mpfr_any(&a, a_exps[i], a_limbs + (size_t)i * n, n) != 0 ||
+        to_mpfr_any(&b, b_exps[i], b_limbs + (size_t)i * n, n) != 0) { bad++; continue; }
+    const int c = mpfr_cmp(&a, &b);
+    r[i] = c > 0 ? 1 : (c < 0 ? -1 : 0);
+  }
+  mpfr_clear(&a); mpfr_clear(&b);
+  return bad;
+}
+
+int gold_neg(uint32_t n, uint32_t count, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *a_exps,
+             const uint32_t *a_limbs) {
+  mpfr_s a, r;
+  mpfr_init2(&a, 32L * n); mpfr_init2(&r, 32L * n);
+  int bad = 0;
+  for (uint32_t i = 0; i < count; i++) {
+    if (to_mpfr_any(&a, a_exps[i], a_limbs + (size_t)i * n, n) != 0) { bad++; continue; }
+    mpfr_neg(&r, &a, RNDN);
+    if (from_mpfr_any(r_exps + i, r_limbs + (size_t)i * n, n, &r) != 0) bad++;
+  }
+  mpfr_clear(&a); mpfr_clear(&r);
+  return bad;
 }

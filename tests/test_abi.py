@@ -77,3 +77,11 @@ def test_configs_cover_all_precisions(lib):
         c = fpa.get_config(n)
         g, k, r = cfgs[c]
         assert g * k * r >= max(n, 4)
+
+
+def test_c_caller_compiles_and_links(lib, tmp_path):
+    """A plain C program written against include/fpa.h (the reference caller's flow,
+    fpa_test.c:283-306) compiles with gcc and links against libfpa_gb300.so."""
+    import c_build
+    exe = c_build.build(tmp_path)
+    assert os.path.exists(exe)

@@ -1,11 +1,15 @@
 """GPU: fpa_batch_run_noalloc, the batched run that allocates nothing.
 
-Callers that may not allocate GPU memory while they compute (a stream being captured into
-a graph, a serving loop that must not wait on the allocator, a host that fixes the
-library's memory footprint) use this entry point with device buffers they already own.
-This test calls it through the C ABI twice in a row, on two different mixed batches, and
-requires each result to equal what the allocating entry point (fpa_batch_create +
-fpa_batch_run) produces for the same inputs, bit for bit.  It also checks the size limit.
+Some callers must not allocate GPU memory where they compute: a serving loop whose latency
+budget cannot absorb cudaMalloc / cudaFree (which may synchronize the device), or a host
+application that hands all device memory to its own allocator up front.  They call this
+entry point with device buffers they already own, and its working memory is a fixed device
+array inside the library.  This test calls it through the C ABI twice in a row, on two
+different mixed batches, and requires each result to equal what the allocating entry point
+(fpa_batch_create + fpa_batch_run) produces for the same inputs, bit for bit, with the
+error word clear after each call.  It also checks that a batch larger than the fixed array
+is rejected.  The file is collected last so that a run stopping at the first failure has
+run every other test before it.
 """
 import ctypes
 
