@@ -31,12 +31,21 @@ State g_state;
 struct DevCtx {
   int sms;
   uint32_t *err;
+  cudaMemPool_t pool;      // stream-ordered scratch of the one-thread div/sqrt kernels
 };
 PerDevice<DevCtx> g_dev;
 
+bool devctx(DevCtx &c);
 bool ctx(int &sms, uint32_t *&err);
 
 }  // namespace
+
+bool gfpa_scratch_pool(cudaMemPool_t *pool) {
+  DevCtx c{};
+  if (!devctx(c)) return false;
+  *pool = c.pool;
+  return true;
+}
 
 bool gfpa_context(int *sms, uint32_t **err) {
   int s; uint32_t *e;
@@ -61,21 +70,33 @@ int gfpa_cfg_for_op(int op, uint32_t n) {
 namespace {
 
 // the current device's context (made with that device current on first use)
+bool devctx(DevCtx &c) {
+  return g_dev.get([](int &dev) { return cudaGetDevice(&dev) == cudaSuccess; },
+                   [](int dev, DevCtx &v) {
+                     int n;
+                     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
+                     uint32_t *e;
+                     if (cudaMalloc(&e, sizeof(uint32_t)) != cudaSuccess) return false;
+                     if (cudaMemset(e, 0, sizeof(uint32_t)) != cudaSuccess) { cudaFree(e); return false; }
+                     // the library's own pool, which keeps what it reserved (no release back
+                     // to the driver at synchronizations)
+                     cudaMemPoolProps props = {};
+                     props.allocType = cudaMemAllocationTypePinned;
+                     props.location.type = cudaMemLocationTypeDevice;
+                     props.location.id = dev;
+                     cudaMemPool_t pool;
+                     if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) { cudaFree(e); return false; }
+                     uint64_t keep = ~0ull;
+                     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+                     v.sms = n; v.err = e; v.pool = pool;
+                     return true;
+                   },
+                   c);
+}
+
 bool ctx(int &sms, uint32_t *&err) {
   DevCtx c{};
-  const bool ok = g_dev.get([](int &dev) { return cudaGetDevice(&dev) == cudaSuccess; },
-                            [](int dev, DevCtx &v) {
-                              int n;
-                              if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-                                return false;
-                              uint32_t *e;
-                              if (cudaMalloc(&e, sizeof(uint32_t)) != cudaSuccess) return false;
-                              if (cudaMemset(e, 0, sizeof(uint32_t)) != cudaSuccess) { cudaFree(e); return false; }
-                              v.sms = n; v.err = e;
-                              return true;
-                            },
-                            c);
-  if (!ok) return false;
+  if (!devctx(c)) return false;
   sms = c.sms; err = c.err;
   return true;
 }

@@ -20,7 +20,7 @@ struct ElementwiseArgs {
   uint32_t kara_min = 0xFFFFFFFFu;   // mul: Karatsuba split from this many limbs (tile >= 8)
 };
 
-#define GFPA_NUM_CFGS 18
+#define GFPA_NUM_CFGS 20
 #define GFPA_OP_FMA 5        // elementwise operation code of fma (after add, sub, mul, div, sqrt)
 #define GFPA_NUM_DEFAULT_CFGS 7
 #define GFPA_MAX_LIMBS 512
@@ -31,17 +31,23 @@ struct ElementwiseArgs {
 // Lane-group configurations (G lanes x K limbs per tile x R block pairs per lane, capacity
 // G*K*R limbs).  0..6 are the defaults in increasing capacity; 7..15 put two to eight
 // operations in one warp (fewer lanes per operation, wider tiles or several block pairs
-// per lane), which the autotuner can choose (mostly for div/sqrt); 16 and 17 are elementwise
-// only (fpa_addsub_narrow.cu): 16 runs add/sub and mul, one thread per operation on
-// shared-memory rows for 8, 16 and 32 limbs and lane groups otherwise; 17 runs add/sub on
-// four lanes x 16 limbs in registers.
-static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4, 4, 4};
-static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4, 8, 16};
-static const int gfpa_cfg_R[GFPA_NUM_CFGS] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 2, 4, 2, 8, 1, 1};
+// per lane), which the autotuner can choose (mostly for div/sqrt); 16 to 19 are elementwise
+// only: 16 runs add/sub and mul, one thread per operation on shared-memory rows for 8, 16
+// and 32 limbs and lane groups otherwise; 17 runs add/sub on four lanes x 16 limbs in
+// registers (fpa_addsub_narrow.cu); 18 and 19 run div and sqrt with one thread per
+// operation and 8x8-limb product tiles, up to 128 and 64 limbs (fpa_thread_newton.cu).
+static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4, 4, 4, 1, 1};
+static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4, 8, 16, 8, 8};
+static const int gfpa_cfg_R[GFPA_NUM_CFGS] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 2, 4, 2, 4, 2, 8, 1, 1, 16, 8};
 static inline int gfpa_cfg_capacity(int c) { return gfpa_cfg_G[c] * gfpa_cfg_K[c] * gfpa_cfg_R[c]; }
-// configurations 16 (add/sub/mul) and 17 (add/sub) have elementwise kernels only
+// configurations 16 to 19 have elementwise kernels only
 static inline bool gfpa_cfg_elementwise_only(int c) { return c >= 16; }
-static inline bool gfpa_cfg_supports(int c, int op) { return c < 16 || op <= 1 || (c == 16 && op == 2); }
+static inline bool gfpa_cfg_supports(int c, int op) {
+  if (c >= 18) return op == 3 || op == 4;
+  return c < 16 || op <= 1 || (c == 16 && op == 2);
+}
+// the current device's memory pool for stream-ordered scratch (fpa_api.cu)
+bool gfpa_scratch_pool(cudaMemPool_t *pool);
 
 extern "C" {
 cudaError_t gfpa_launch_cfg0(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
@@ -62,6 +68,8 @@ cudaError_t gfpa_launch_cfg14(int op, const ElementwiseArgs *args, cudaStream_t 
 cudaError_t gfpa_launch_cfg15(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 cudaError_t gfpa_launch_cfg16(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 cudaError_t gfpa_launch_cfg17(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg18(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
+cudaError_t gfpa_launch_cfg19(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms);
 }
 
 // smallest default configuration whose capacity holds n limbs
@@ -91,6 +99,8 @@ static inline cudaError_t gfpa_launch(int cfg, int op, const ElementwiseArgs *ar
     case 15: return gfpa_launch_cfg15(op, args, stream, sms);
     case 16: return gfpa_launch_cfg16(op, args, stream, sms);
     case 17: return gfpa_launch_cfg17(op, args, stream, sms);
+    case 18: return gfpa_launch_cfg18(op, args, stream, sms);
+    case 19: return gfpa_launch_cfg19(op, args, stream, sms);
   }
   return cudaErrorInvalidValue;
 }

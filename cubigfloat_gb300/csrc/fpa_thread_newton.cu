@@ -1,0 +1,111 @@
+// fpa_thread_newton.cu -- elementwise div and sqrt with one thread per operation
+// (configurations 18 and 19: up to 128 and up to 64 limbs).
+//
+// A CTA is one warp; each thread runs whole operations (tdiv / tsqrt of
+// fpa_thread_newton.cuh) in its columns of the warp's shared-memory workspace.  An
+// operation whose extra-limb quotient or root lies within the rounding margin needs the
+// exact correction, a full n x n product on one thread: done inline it would keep the other
+// 31 threads of its warp waiting, and with a few percent of such operations most warps
+// would carry one.  So the first pass only appends their indices to a list (one atomic per
+// warp) and writes nothing for them, and a second pass runs the listed operations again
+// with the exact correction, 32 at a time.  The list is stream-ordered scratch from the
+// library's memory pool (4 bytes per operation), so concurrent calls on different streams
+// never share it.
+#include <cuda_runtime.h>
+#include "fpa_thread_newton.cuh"
+#include "fpa_launch.h"
+
+namespace gfpa {
+
+template <int OP, int N>
+__global__ void __launch_bounds__(32) k_tnewton(ElementwiseArgs args, uint32_t *hard_count, uint32_t *hard_idx,
+                                                int pass) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  const uint32_t lane = threadIdx.x;
+  uint32_t *w = smem + lane;                          // this thread's columns
+  const int n = (int)args.n;
+  const uint64_t total = (uint64_t)gridDim.x * 32;
+  auto run = [&](uint64_t i, bool exact) -> int {
+    const uint64_t off = i * (uint64_t)n;
+    if (OP == OP_DIV)
+      return tdiv<N>(w, n, args.mode, args.a_exps[i], args.a_limbs + off, args.b_exps[i], args.b_limbs + off,
+                     args.r_exps + i, args.r_limbs + off, exact, args.err);
+    return tsqrt<N>(w, n, args.mode, args.a_exps[i], args.a_limbs + off, args.r_exps + i, args.r_limbs + off, exact,
+                    args.err);
+  };
+  if (pass == 0) {
+    const uint64_t iters = (args.count + total - 1) / total;
+    for (uint64_t it = 0; it < iters; it++) {         // the same trip count on every thread
+      const uint64_t i = it * total + (uint64_t)blockIdx.x * 32 + lane;
+      const int hard = (i < args.count) ? run(i, false) : 0;
+      const uint32_t mask = __ballot_sync(0xFFFFFFFFu, hard != 0);
+      if (mask) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(hard_count, (uint32_t)__popc(mask));
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (hard) hard_idx[base + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)i;
+      }
+    }
+  } else {
+    const uint64_t cnt = *hard_count;
+    for (uint64_t j = (uint64_t)blockIdx.x * 32 + lane; j < cnt; j += total) run(hard_idx[j], true);
+  }
+}
+
+template <int OP, int N>
+static cudaError_t launch_tnewton(const ElementwiseArgs &args, cudaStream_t stream, int sms) {
+  constexpr size_t smem = (size_t)32 * TSpace<N>::words * sizeof(uint32_t);
+  static_assert(smem <= 227 * 1024, "one warp's workspace must fit a CTA");
+  auto kern = k_tnewton<OP, N>;
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int blocks = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, 32, smem);
+    if (e != cudaSuccess) return e;
+    per_sm = blocks > 0 ? blocks : 1;
+  }
+  const uint64_t need = (args.count + 31) / 32, cap = (uint64_t)sms * (uint64_t)per_sm;
+  const unsigned grid = (unsigned)(need < cap ? need : cap);
+  if (grid == 0) return cudaSuccess;
+  cudaMemPool_t pool;
+  if (!gfpa_scratch_pool(&pool)) return cudaErrorMemoryAllocation;
+  uint32_t *list = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync((void **)&list, (size_t)(args.count + 1) * sizeof(uint32_t), pool, stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(list, 0, sizeof(uint32_t), stream);
+  if (e == cudaSuccess) {
+    kern<<<grid, 32, smem, stream>>>(args, list, list + 1, 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    kern<<<grid, 32, smem, stream>>>(args, list, list + 1, 1);
+    e = cudaGetLastError();
+  }
+  const cudaError_t ef = cudaFreeAsync(list, stream);
+  return e != cudaSuccess ? e : ef;
+}
+
+template <int N>
+static cudaError_t launch_cfg(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms) {
+  if ((int)args->n > N) return cudaErrorInvalidValue;
+  if ((int)args->n < TSpace<N>::min_limbs) {           // small numbers: the lane-group kernels
+    const int c = gfpa_default_cfg(args->n < 4 ? 4 : args->n);
+    return c < 0 ? cudaErrorInvalidValue : gfpa_launch(c, op, args, stream, sms);
+  }
+  switch (op) {
+    case OP_DIV: return launch_tnewton<OP_DIV, N>(*args, stream, sms);
+    case OP_SQRT: return launch_tnewton<OP_SQRT, N>(*args, stream, sms);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace gfpa
+
+extern "C" cudaError_t gfpa_launch_cfg18(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms) {
+  return gfpa::launch_cfg<128>(op, args, stream, sms);
+}
+extern "C" cudaError_t gfpa_launch_cfg19(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms) {
+  return gfpa::launch_cfg<64>(op, args, stream, sms);
+}

@@ -65,9 +65,9 @@ def test_argument_checks_without_device(lib):
     x = fpa.fpa_s()
     assert lib.fpa_init(P(x), 10, 1000) == fpa.fpa_invalid_precisions
     assert lib.fpa_init(P(x), 10, 16416) == fpa.fpa_invalid_precisions
-    assert lib.fpa_gb300_num_configs() == 18
+    assert lib.fpa_gb300_num_configs() == 20
     c128 = lib.fpa_gb300_get_config(128)       # the autotuned table's choice, or the default (4)
-    assert 0 <= c128 < 18 and np.prod(fpa.configs()[c128]) >= 128
+    assert 0 <= c128 < 20 and np.prod(fpa.configs()[c128]) >= 128
     assert lib.fpa_gb300_get_config(513) == -1
 
 

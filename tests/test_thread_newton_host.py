@@ -1,0 +1,195 @@
+"""The one-thread-per-operation div and sqrt (tdiv / tsqrt in
+cubigfloat_gb300/csrc/fpa_thread_newton.cuh, with tmul, tround_store and the Newton
+building blocks of fpa_ops.cuh under them), compiled for the host from the device source,
+bit-exact against the oracle in every rounding mode, at 8 to 128 limbs, on random operands,
+the reference generator's limb pattern, near-exact quotients and squares, all-ones
+mantissas and every special class.  Each operation first runs without the exact correction;
+one that reports it needs the correction runs again with it, as the kernel's second pass
+does, and both outcomes are checked.  The GPU tests run the same functions in the kernels."""
+import os
+import re
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from cubigfloat_gb300 import workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, "cubigfloat_gb300", "csrc")
+
+SHIMS = r"""
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+using std::min;
+using std::max;
+static inline int __clz(int v) { return v == 0 ? 32 : __builtin_clz((unsigned)v); }
+static inline uint32_t atomicOr(uint32_t *p, uint32_t v) { const uint32_t o = *p; *p |= v; return o; }
+namespace gfpa {
+// mad.lo.cc / madc.hi.cc / addc: (lo, hi, tp) += a * b
+static inline void mac3(uint32_t &lo, uint32_t &hi, uint32_t &tp, uint32_t a, uint32_t b) {
+  const uint64_t p = (uint64_t)a * b;
+  const uint64_t s0 = (uint64_t)lo + (uint32_t)p;
+  lo = (uint32_t)s0;
+  const uint64_t s1 = (uint64_t)hi + (p >> 32) + (s0 >> 32);
+  hi = (uint32_t)s1;
+  tp += (uint32_t)(s1 >> 32);
+}
+"""
+
+MAIN = r"""
+}  // namespace gfpa
+using namespace gfpa;
+// one operation per input line: op n mode a_exp a[0..n) [b_exp b[0..n)]
+template <int NC>
+static void run(int op, int n, int mode, uint32_t ae, const uint32_t *a, uint32_t be, const uint32_t *b) {
+  std::vector<uint32_t> ws((size_t)32 * TSpace<NC>::words + 64, 0xA5A5A5A5u), r(n, 0);
+  uint32_t re = 0, err = 0;
+  int hard = op == 3 ? tdiv<NC>(ws.data(), n, mode, ae, a, be, b, &re, r.data(), false, &err)
+                     : tsqrt<NC>(ws.data(), n, mode, ae, a, &re, r.data(), false, &err);
+  if (hard) {
+    std::fill(ws.begin(), ws.end(), 0x5A5A5A5Au);
+    const int again = op == 3 ? tdiv<NC>(ws.data(), n, mode, ae, a, be, b, &re, r.data(), true, &err)
+                              : tsqrt<NC>(ws.data(), n, mode, ae, a, &re, r.data(), true, &err);
+    if (again) { printf("ERROR exact pass reported hard\n"); return; }
+  }
+  printf("%d %u %u", hard, err, re);
+  for (int i = 0; i < n; i++) printf(" %u", re > CLS_SNAN ? r[i] : 0u);
+  printf("\n");
+}
+int main() {
+  int op, n, mode;
+  while (scanf("%d %d %d", &op, &n, &mode) == 3) {
+    std::vector<uint32_t> a(n), b(n);
+    unsigned ae, be = 0;
+    if (scanf("%u", &ae) != 1) return 1;
+    for (int i = 0; i < n; i++) { unsigned x; if (scanf("%u", &x) != 1) return 1; a[i] = x; }
+    if (op == 3) {
+      if (scanf("%u", &be) != 1) return 1;
+      for (int i = 0; i < n; i++) { unsigned x; if (scanf("%u", &x) != 1) return 1; b[i] = x; }
+    }
+    if (n <= 64) run<64>(op, n, mode, ae, a.data(), be, b.data());
+    else run<128>(op, n, mode, ae, a.data(), be, b.data());
+  }
+  return 0;
+}
+"""
+
+
+def extract(src, start, end):
+    a = src.index(start)
+    b = src.index(end, a)
+    return src[a:b]
+
+
+def host_source():
+    dev = open(os.path.join(CSRC, "fpa_device.cuh")).read()
+    ops = open(os.path.join(CSRC, "fpa_ops.cuh")).read()
+    tn = open(os.path.join(CSRC, "fpa_thread_newton.cuh")).read()
+    div_mark = "// ---------------------------------------------------------------------------------------\n// div."
+    sqrt_mark = "// ---------------------------------------------------------------------------------------\n// sqrt."
+    parts = [
+        extract(dev, "constexpr uint32_t BIAS", "// Special-value tables"),
+        extract(dev, "static __constant__ uint8_t c_action", "__device__ __forceinline__ uint32_t classify"),
+        extract(dev, "__device__ __forceinline__ uint32_t classify", "// ----"),
+        extract(dev, "__device__ __forceinline__ uint32_t clz32", "\n") + "\n",
+        extract(dev, "// (lo,hi,tp)[c] columns -> K+2 limbs", "template <int G, int K, int R>\n__device__"),
+        extract(ops, "// exponent word from an unbiased exponent", "// ----"),
+        extract(ops, "// Newton level schedule", "// Newton residual magnitude"),
+        extract(ops, "constexpr int SMALL_LEVEL", div_mark),
+        extract(ops, "// integer square root of a 64-bit value", sqrt_mark),
+        extract(tn, "constexpr int TS = 32;", "}  // namespace gfpa"),
+    ]
+    body = "\n".join(parts)
+    body = body.replace("static __constant__", "static const")
+    body = re.sub(r"__device__\s+__forceinline__", "inline", body)
+    body = re.sub(r"__device__\s+__noinline__", "", body)
+    body = re.sub(r"__device__", "", body)
+    body = body.replace("#pragma unroll 1", "").replace("#pragma unroll", "")
+    return SHIMS + body + MAIN
+
+
+@pytest.fixture(scope="module")
+def host_binary(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not found")
+    d = tmp_path_factory.mktemp("tnewton")
+    src, exe = d / "tnewton.cpp", d / "tnewton"
+    src.write_text(host_source())
+    r = subprocess.run([cxx, "-O2", "-std=c++17", "-o", str(exe), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    return str(exe)
+
+
+def run_host(exe, op, n, mode, ae, al, be=None, bl=None):
+    lines = []
+    for i in range(len(ae)):
+        s = f"{op} {n} {mode} {int(ae[i])} " + " ".join(map(str, al[i]))
+        if op == 3:
+            s += f" {int(be[i])} " + " ".join(map(str, bl[i]))
+        lines.append(s)
+    out = subprocess.run([exe], input="\n".join(lines) + "\n", capture_output=True, text=True, check=True).stdout
+    assert "ERROR" not in out, out[:500]
+    rows = np.array([[int(x) for x in line.split()] for line in out.strip().split("\n")], dtype=np.uint64)
+    return rows[:, 0].astype(int), rows[:, 1].astype(np.uint32), rows[:, 2].astype(np.uint32), \
+        rows[:, 3:].astype(np.uint32)
+
+
+def cases(op, n, seed, count=24):
+    rng = np.random.default_rng(seed)
+    ae, al = W.uniform(rng, count, n, -300, 300, signs=(op == 3))
+    be, bl = W.uniform(rng, count, n, -300, 300)
+    re_a, rl_a = W.reference_style(rng, 8, n)
+    re_b, rl_b = W.reference_style(rng, 8, n)
+    hard_a, hard_b, hard_ea = [], [], []
+    for _ in range(8):
+        if op == 3:
+            A, B = W.div_near_exact(rng, n)
+            hard_a.append(W.int_to_limbs(A, n)); hard_b.append(W.int_to_limbs(B, n))
+            hard_ea.append(W.exp_word(int(rng.integers(-9, 9)), int(rng.integers(0, 2))))
+        else:
+            A, par = W.sqrt_near_exact(rng, n)
+            hard_a.append(W.int_to_limbs(A, n)); hard_b.append(W.int_to_limbs(A, n))
+            hard_ea.append(W.exp_word(2 * int(rng.integers(-9, 9)) + par, 0))
+    ones = np.full((2, n), 0xFFFFFFFF, np.uint32)
+    ae = np.concatenate([ae, re_a, np.array(hard_ea, np.uint32), W.exp_word(np.array([3, -4]), 0)])
+    al = np.concatenate([al, rl_a, np.stack(hard_a), ones])
+    be = np.concatenate([be, re_b, W.exp_word(rng.integers(-9, 9, 8), rng.integers(0, 2, 8)),
+                         W.exp_word(np.array([1, 2]), 0)])
+    bl = np.concatenate([bl, rl_b, np.stack(hard_b), ones])
+    if op == 4:
+        ae = ae & ~np.uint32(1)
+    # special classes against a value and each other
+    sp_e, sp_l = W.specials(n)
+    ae = np.concatenate([ae, sp_e, np.repeat(sp_e[:1], sp_e.size)])
+    al = np.concatenate([al, sp_l, np.repeat(sp_l[:1], sp_e.size, axis=0)])
+    be = np.concatenate([be, np.repeat(sp_e[:1], sp_e.size), sp_e])
+    bl = np.concatenate([bl, np.repeat(sp_l[:1], sp_e.size, axis=0), sp_l])
+    return ae, al, be, bl
+
+
+SIZES = [8, 9, 15, 16, 17, 31, 32, 33, 48, 63, 64, 65, 100, 127, 128]
+
+
+@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("op", [3, 4], ids=["div", "sqrt"])
+def test_thread_newton_matches_oracle(host_binary, op, n):
+    ae, al, be, bl = cases(op, n, 7000 + 10 * n + op)
+    seen_hard = 0
+    for mode in range(5):
+        hard, err, ge, gl = run_host(host_binary, op, n, mode, ae, al, be, bl)
+        ee, el = oracle.run(op, n, mode, ae, al, be, bl)
+        assert (err == 0).all()
+        bad = np.flatnonzero(ge != ee)
+        assert bad.size == 0, (op, n, mode, int(bad[0]), hex(int(ge[bad[0]])), hex(int(ee[bad[0]])))
+        val = ee > 8
+        badl = np.flatnonzero(np.any(gl != el, axis=1) & val)
+        assert badl.size == 0, (op, n, mode, int(badl[0]))
+        seen_hard += int(hard.sum())
+    # the near-exact cases take the exact correction
+    assert seen_hard > 0

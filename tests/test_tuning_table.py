@@ -9,10 +9,12 @@ from cubigfloat_gb300 import tune
 # (lanes, tile limbs, block pairs) per configuration, as in csrc/fpa_launch.h
 SHAPES = [(4, 2, 1), (8, 2, 1), (8, 4, 1), (16, 4, 1), (32, 4, 1), (32, 8, 1), (32, 16, 1), (16, 8, 1),
           (8, 16, 1), (16, 16, 1), (8, 4, 2), (8, 4, 4), (16, 4, 2), (8, 8, 4), (16, 8, 2), (4, 4, 8),
-          (4, 8, 1), (4, 16, 1)]
+          (4, 8, 1), (4, 16, 1), (1, 8, 16), (1, 8, 8)]
 
 
 def supports(cfg, op):
+    if cfg >= 18:                      # one thread per operation: div and sqrt
+        return op in (3, 4)
     return cfg < 16 or op <= 1 or (cfg == 16 and op == 2)
 
 
