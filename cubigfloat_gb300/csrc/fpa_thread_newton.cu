@@ -8,9 +8,9 @@
 // 31 threads of its warp waiting, and with a few percent of such operations most warps
 // would carry one.  So the first pass only appends their indices to a list (one atomic per
 // warp) and writes nothing for them, and a second pass runs the listed operations again
-// with the exact correction, 32 at a time.  The list is stream-ordered scratch from the
-// library's memory pool (4 bytes per operation), so concurrent calls on different streams
-// never share it.
+// with the exact correction, 32 at a time.  The list (4 bytes per operation) and the
+// operand slabs (one per CTA, fpa_thread_newton.cuh) are stream-ordered scratch from the
+// library's memory pool, so concurrent calls on different streams never share them.
 #include <cuda_runtime.h>
 #include "fpa_thread_newton.cuh"
 #include "fpa_launch.h"
@@ -19,18 +19,19 @@ namespace gfpa {
 
 template <int OP, int N>
 __global__ void __launch_bounds__(32) k_tnewton(ElementwiseArgs args, uint32_t *hard_count, uint32_t *hard_idx,
-                                                int pass) {
+                                                uint32_t *slabs, int pass) {
   extern __shared__ __align__(16) uint32_t smem[];
   const uint32_t lane = threadIdx.x;
   uint32_t *w = smem + lane;                          // this thread's columns
+  uint32_t *slab = slabs + (size_t)blockIdx.x * 32 * TSpace<N>::slab + lane;
   const int n = (int)args.n;
   const uint64_t total = (uint64_t)gridDim.x * 32;
   auto run = [&](uint64_t i, bool exact) -> int {
     const uint64_t off = i * (uint64_t)n;
     if (OP == OP_DIV)
-      return tdiv<N>(w, n, args.mode, args.a_exps[i], args.a_limbs + off, args.b_exps[i], args.b_limbs + off,
+      return tdiv<N>(w, slab, n, args.mode, args.a_exps[i], args.a_limbs + off, args.b_exps[i], args.b_limbs + off,
                      args.r_exps + i, args.r_limbs + off, exact, args.err);
-    return tsqrt<N>(w, n, args.mode, args.a_exps[i], args.a_limbs + off, args.r_exps + i, args.r_limbs + off, exact,
+    return tsqrt<N>(w, slab, n, args.mode, args.a_exps[i], args.a_limbs + off, args.r_exps + i, args.r_limbs + off, exact,
                     args.err);
   };
   if (pass == 0) {
@@ -71,16 +72,20 @@ static cudaError_t launch_tnewton(const ElementwiseArgs &args, cudaStream_t stre
   if (grid == 0) return cudaSuccess;
   cudaMemPool_t pool;
   if (!gfpa_scratch_pool(&pool)) return cudaErrorMemoryAllocation;
+  // hard-operation list (count + 1 words), then one operand slab per CTA
+  const size_t list_bytes = ((size_t)(args.count + 1) * sizeof(uint32_t) + 255) & ~(size_t)255;
+  const size_t slab_bytes = (size_t)grid * 32 * TSpace<N>::slab * sizeof(uint32_t);
   uint32_t *list = nullptr;
-  cudaError_t e = cudaMallocFromPoolAsync((void **)&list, (size_t)(args.count + 1) * sizeof(uint32_t), pool, stream);
+  cudaError_t e = cudaMallocFromPoolAsync((void **)&list, list_bytes + slab_bytes, pool, stream);
   if (e != cudaSuccess) return e;
+  uint32_t *slabs = list + list_bytes / sizeof(uint32_t);
   e = cudaMemsetAsync(list, 0, sizeof(uint32_t), stream);
   if (e == cudaSuccess) {
-    kern<<<grid, 32, smem, stream>>>(args, list, list + 1, 0);
+    kern<<<grid, 32, smem, stream>>>(args, list, list + 1, slabs, 0);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    kern<<<grid, 32, smem, stream>>>(args, list, list + 1, 1);
+    kern<<<grid, 32, smem, stream>>>(args, list, list + 1, slabs, 1);
     e = cudaGetLastError();
   }
   const cudaError_t ef = cudaFreeAsync(list, stream);

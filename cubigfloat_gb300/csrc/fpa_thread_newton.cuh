@@ -24,8 +24,13 @@
 // result with the half-size quotient / root placed at its final offset), 2N+24 words.
 //
 // Operands a, b and the result r are the caller's arrays in the natural layout (number i's
-// limbs contiguous).  Reference semantics as op_div / op_sqrt: fpa_warp_div.h:127-201,
-// fpa_warp_sqrt.h:195-254.
+// limbs contiguous).  A thread reading its own number touches one 32-byte sector per limb
+// read across the warp's 32 numbers, and the products read the operands many times, so
+// each operation first copies its operands once into a slab in global memory laid out
+// like the workspace (limb j of this thread at slab[32*j]): A and B for div, Xh =
+// floor(A * 2^(32-odd)) for sqrt.  Every later operand read is then one coalesced 128-byte
+// warp load, and sqrt's shifted operand costs no shifts.  Reference semantics as op_div /
+// op_sqrt: fpa_warp_div.h:127-201, fpa_warp_sqrt.h:195-254.
 #pragma once
 #include "fpa_ops.cuh"
 
@@ -38,29 +43,26 @@ struct TSpace {
   static constexpr int H = N / 2 + 8;        // R0, R1
   static constexpr int Q = N + 8;            // R3
   static constexpr int words = 2 * H + Q;    // per thread
+  static constexpr int slab = 2 * N + 8;     // operand slab words per thread (global memory)
   static constexpr int min_limbs = 8;        // smaller numbers keep the lane-group path
 };
 
+// Copies n limbs of a natural-layout number to a slab column (limb j at dst[TS*j]).
+__device__ __forceinline__ void stage_limbs(uint32_t *dst, const uint32_t *src, int n) {
+  if ((((uintptr_t)src) & 15) == 0 && (n & 3) == 0) {
+    for (int j = 0; j < n; j += 4) {
+      const uint4 v = *reinterpret_cast<const uint4 *>(src + j);
+      dst[TS * j] = v.x; dst[TS * (j + 1)] = v.y; dst[TS * (j + 2)] = v.z; dst[TS * (j + 3)] = v.w;
+    }
+  } else {
+    for (int j = 0; j < n; j++) dst[TS * j] = src[j];
+  }
+}
+
 // ---- operand views: limb i of a number, 0 outside [0, len) ---------------------------
-struct VW {                     // a workspace buffer
+struct VW {                     // a workspace buffer or a slab column
   const uint32_t *p; int len;
   __device__ __forceinline__ uint32_t get(int i) const { return ((unsigned)i < (unsigned)len) ? p[TS * i] : 0u; }
-};
-struct VG {                     // natural layout (the caller's arrays)
-  const uint32_t *p; int len;
-  __device__ __forceinline__ uint32_t get(int i) const { return ((unsigned)i < (unsigned)len) ? p[i] : 0u; }
-};
-// limbs [off, off+len) of Xh = floor(A * 2^(32 - odd)) (n+1 limbs), A natural layout
-struct VXh {
-  const uint32_t *a; int n, odd, off, len;
-  __device__ __forceinline__ uint32_t get(int i) const {
-    if ((unsigned)i >= (unsigned)len) return 0u;
-    const int j = off + i;
-    const uint32_t lo = (j >= 1 && j <= n) ? a[j - 1] : 0u;
-    if (!odd) return lo;
-    const uint32_t hi = (j < n) ? a[j] : 0u;
-    return (lo >> 1) | (hi << 31);
-  }
 };
 // the Newton residual magnitude (ResidualMag) read from raw product limbs T[off ...] that
 // were stored from index 0: limb i is T[i] (or ~T[i] when the product was below 2^(32L)),
@@ -161,24 +163,27 @@ __device__ __forceinline__ int tround_store(const uint32_t *X, int xlen, int n, 
 // rounding margin and `exact` is false: the operation then needs the exact correction
 // (the caller runs it again with exact = true; nothing has been written).
 template <int N>
-__device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t *a, uint32_t b_exp,
+__device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp, const uint32_t *a, uint32_t b_exp,
                     const uint32_t *b, uint32_t *r_exp, uint32_t *r, bool exact, uint32_t *err) {
   constexpr int H = TSpace<N>::H;
   const uint32_t act = c_action[3][classify(a_exp) * 9 + classify(b_exp)];
   if (act != ACT_DIV) { *r_exp = act; return 0; }
   uint32_t *R0 = w, *R1 = w + TS * H, *R3 = w + TS * 2 * H;
+  uint32_t *SA = slab, *SB = slab + TS * n;          // A and B, limb j at [TS*j]
+  stage_limbs(SA, a, n);
+  stage_limbs(SB, b, n);
   int lv[24];
   const int nl = newton_levels(n, lv);
   const int l0 = small_levels_end(lv, nl, true);
   uint32_t *Y = R0, *Y2 = R1;
   {
-    const uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)b[n - 1];   // level 1: floor((2^64-1)/B_top)
+    const uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)SB[TS * (n - 1)];   // level 1: floor((2^64-1)/B_top)
     uint32_t v[SMALL_LEVEL + 1], bt[SMALL_LEVEL];
 #pragma unroll
     for (int i = 0; i <= SMALL_LEVEL; i++) v[i] = 0u;
     v[0] = (uint32_t)y; v[1] = (uint32_t)(y >> 32);
 #pragma unroll
-    for (int i = 0; i < SMALL_LEVEL; i++) bt[i] = (n - SMALL_LEVEL + i >= 0) ? b[n - SMALL_LEVEL + i] : 0u;
+    for (int i = 0; i < SMALL_LEVEL; i++) bt[i] = (n - SMALL_LEVEL + i >= 0) ? SB[TS * (n - SMALL_LEVEL + i)] : 0u;
     small_levels<false>(bt, lv, l0, v);
     const int k = lv[l0 - 1];
 #pragma unroll
@@ -187,7 +192,7 @@ __device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t
   for (int li = l0; li < nl - 1; li++) {
     const int k = lv[li - 1], kp = lv[li], L = k + kp, lt = kp - k + 3;
     // T = B_k' * Y_k: keep limbs k-1 .. L (the lower ones reach them only through carries)
-    tmul(VG{b + (n - kp), kp}, kp, VW{Y, k + 1}, k + 1, L + 1, [&](int cb, const uint32_t (&o)[10]) {
+    tmul(VW{SB + TS * (n - kp), kp}, kp, VW{Y, k + 1}, k + 1, L + 1, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         const int j = 8 * cb + q - (k - 1);
@@ -219,7 +224,7 @@ __device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t
   // level, m = n+2-h; q0 is placed at limb h-1 of R3 so that Q' forms in place.
   const int h = lv[nl - 2], m = n + 2 - h;
   uint32_t *D = Y2, *Q = R3;
-  tmul(VG{a + (n - m - 1), m + 1}, m + 1, VW{Y, h + 1}, h + 1, h + 2 + m, [&](int cb, const uint32_t (&o)[10]) {
+  tmul(VW{SA + TS * (n - m - 1), m + 1}, m + 1, VW{Y, h + 1}, h + 1, h + 2 + m, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int j = 8 * cb + q - (h + 1);
@@ -229,12 +234,12 @@ __device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t
   // D = |A 2^96 - floor(q0 B / 2^(32(n-h-1)))| over n+4 limbs, its low m+2 limbs kept
   const int dl = n + 4, dlen = m + 2, sh = n - h - 1;
   uint32_t bw = 0u;
-  tmul(VW{Q + TS * (h - 1), m + 1}, m + 1, VG{b, n}, n, n + m + 1, [&](int cb, const uint32_t (&o)[10]) {
+  tmul(VW{Q + TS * (h - 1), m + 1}, m + 1, VW{SB, n}, n, n + m + 1, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q - sh;
       if (i >= 0 && i < dl) {
-        const uint32_t xa = (i >= 3 && i - 3 < n) ? a[i - 3] : 0u, xq = o[q];
+        const uint32_t xa = (i >= 3 && i - 3 < n) ? SA[TS * (i - 3)] : 0u, xq = o[q];
         const uint32_t v = xa - xq - bw;
         bw = (xa < xq || (xa == xq && bw)) ? 1u : 0u;
         if (i < dlen) D[TS * i] = v;
@@ -286,17 +291,22 @@ __device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t
   uint32_t c1 = 0u, b2 = 0u;
   auto putr = [&](int i, uint32_t p) {
     // P2 = Q[0..n) B + (qt B) 2^(32n): add the small multiple, then subtract from A 2^(32n)
-    const uint32_t smv = (i >= n) ? SmallMul{b, n, qt}(i - n) : 0u;
+    uint32_t smv = 0u;                               // (qt B) 2^(32n), qt in {0, 1, 2, 4}
+    if (i >= n && qt) {
+      const int t = i - n;
+      const uint32_t v = t < n ? SB[TS * t] : 0u, wv = (t >= 1 && t - 1 < n) ? SB[TS * (t - 1)] : 0u;
+      smv = qt == 1 ? v : (qt == 2 ? ((v << 1) | (wv >> 31)) : ((v << 2) | (wv >> 30)));
+    }
     const uint64_t t = (uint64_t)p + smv + c1;
     const uint32_t pv = (uint32_t)t;
     c1 = (uint32_t)(t >> 32);
-    const uint32_t av = (i >= n) ? ((i - n < n) ? a[i - n] : 0u) : 0u;
+    const uint32_t av = (i >= n && i - n < n) ? SA[TS * (i - n)] : 0u;
     const uint32_t v = av - pv - b2;
     b2 = (av < pv || (av == pv && b2)) ? 1u : 0u;
     Rm[TS * i] = v;
   };
   int nextr = 0;
-  tmul(VW{Qc, n}, n, VG{b, n}, n, n + 2, [&](int cb, const uint32_t (&o)[10]) {
+  tmul(VW{Qc, n}, n, VW{SB, n}, n, n + 2, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q;
@@ -311,7 +321,7 @@ __device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t
     for (int i = 0; i <= n && bq; i++) { const uint32_t v = Qc[TS * i]; Qc[TS * i] = v - 1u; bq = v == 0u; }
     uint32_t c = 0u;
     for (int i = 0; i < n + 2; i++) {
-      const uint64_t t = (uint64_t)Rm[TS * i] + (i < n ? b[i] : 0u) + c;
+      const uint64_t t = (uint64_t)Rm[TS * i] + (i < n ? SB[TS * i] : 0u) + c;
       Rm[TS * i] = (uint32_t)t; c = (uint32_t)(t >> 32);
     }
     guard++;
@@ -319,7 +329,7 @@ __device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t
   for (;;) {
     int cmp = 0;
     for (int i = n + 1; i >= 0 && cmp == 0; i--) {
-      const uint32_t x = Rm[TS * i], y = i < n ? b[i] : 0u;
+      const uint32_t x = Rm[TS * i], y = i < n ? SB[TS * i] : 0u;
       if (x != y) cmp = x > y ? 1 : -1;
     }
     if (cmp < 0 || guard >= 64) break;
@@ -327,7 +337,7 @@ __device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t
     for (int i = 0; i <= n && cq2; i++) { const uint32_t v = Qc[TS * i] + 1u; Qc[TS * i] = v; cq2 = v == 0u; }
     uint32_t bb = 0u;
     for (int i = 0; i < n + 2; i++) {
-      const uint32_t x = Rm[TS * i], y = i < n ? b[i] : 0u;
+      const uint32_t x = Rm[TS * i], y = i < n ? SB[TS * i] : 0u;
       Rm[TS * i] = x - y - bb;
       bb = (x < y || (x == y && bb)) ? 1u : 0u;
     }
@@ -338,7 +348,7 @@ __device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t
   int c2 = 0;
   uint32_t nz = 0u;
   for (int i = n + 1; i >= 0; i--) {
-    const uint32_t x = (Rm[TS * i] << 1) | (i > 0 ? (Rm[TS * (i - 1)] >> 31) : 0u), y = i < n ? b[i] : 0u;
+    const uint32_t x = (Rm[TS * i] << 1) | (i > 0 ? (Rm[TS * (i - 1)] >> 31) : 0u), y = i < n ? SB[TS * i] : 0u;
     nz |= Rm[TS * i];
     if (c2 == 0 && x != y) c2 = x > y ? 1 : -1;
   }
@@ -363,7 +373,7 @@ __device__ int tdiv(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t
 // n+1 limbs (read from A on the fly), Newton on 1/sqrt with three products per level, the
 // Karp-Markstein step with one limb more, the exact correction with R = A_ext - S^2.
 template <int N>
-__device__ int tsqrt(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_t *a, uint32_t *r_exp,
+__device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp, const uint32_t *a, uint32_t *r_exp,
                      uint32_t *r, bool exact, uint32_t *err) {
   constexpr int H = TSpace<N>::H;
   const uint32_t act = c_sqrt_action[classify(a_exp)];
@@ -372,7 +382,17 @@ __device__ int tsqrt(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_
   const long long e = (long long)(a_exp >> 1) - BIAS;
   const int odd = (int)(e & 1);
   const long long eh = (e + odd) / 2;
-  const VXh xh{a, n, odd, 0, n + 1};
+  // Xh = floor(A * 2^(32 - odd)), n+1 limbs, staged in the slab
+  {
+    uint32_t prev = 0u;
+    for (int j = 0; j < n; j++) {
+      const uint32_t cur = a[j];
+      slab[TS * j] = odd ? ((prev >> 1) | (cur << 31)) : prev;
+      prev = cur;
+    }
+    slab[TS * n] = odd ? (prev >> 1) : prev;
+  }
+  const VW xh{slab, n + 1};
   int lv[24];
   const int nl = newton_levels(n, lv);
   const int l0 = small_levels_end(lv, nl, true);
@@ -398,7 +418,7 @@ __device__ int tsqrt(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_
     const int j = k > 2 ? k - 2 : 0, l1 = kp + k + 1 - j, L = kp + 2 * k - j, lt = kp - k + 3;
     uint32_t *V1s = R3, *Wr = R3 + TS * WOFF;
     // V1 = X_k' Z_k, kept from limb j up
-    tmul(VXh{a, n, odd, n + 1 - kp, kp}, kp, VW{Z, k + 1}, k + 1, kp + k + 1, [&](int cb, const uint32_t (&o)[10]) {
+    tmul(VW{slab + TS * (n + 1 - kp), kp}, kp, VW{Z, k + 1}, k + 1, kp + k + 1, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         const int i = 8 * cb + q - j;
@@ -442,7 +462,7 @@ __device__ int tsqrt(uint32_t *w, int n, int mode, uint32_t a_exp, const uint32_
   // limb h-1 of R3 so that S' forms in place
   const int h = lv[nl - 2], m = n + 2 - h;
   uint32_t *D = Z2, *S = R3;
-  tmul(VXh{a, n, odd, n - m, m + 1}, m + 1, VW{Z, h + 1}, h + 1, h + 2 + m, [&](int cb, const uint32_t (&o)[10]) {
+  tmul(VW{slab + TS * (n - m), m + 1}, m + 1, VW{Z, h + 1}, h + 1, h + 2 + m, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q - (h + 1);

@@ -29,6 +29,7 @@ using std::min;
 using std::max;
 static inline int __clz(int v) { return v == 0 ? 32 : __builtin_clz((unsigned)v); }
 static inline uint32_t atomicOr(uint32_t *p, uint32_t v) { const uint32_t o = *p; *p |= v; return o; }
+struct uint4 { uint32_t x, y, z, w; };
 namespace gfpa {
 // mad.lo.cc / madc.hi.cc / addc: (lo, hi, tp) += a * b
 static inline void mac3(uint32_t &lo, uint32_t &hi, uint32_t &tp, uint32_t a, uint32_t b) {
@@ -48,13 +49,14 @@ using namespace gfpa;
 template <int NC>
 static void run(int op, int n, int mode, uint32_t ae, const uint32_t *a, uint32_t be, const uint32_t *b) {
   std::vector<uint32_t> ws((size_t)32 * TSpace<NC>::words + 64, 0xA5A5A5A5u), r(n, 0);
+  std::vector<uint32_t> slab((size_t)32 * TSpace<NC>::slab + 64, 0xC3C3C3C3u);
   uint32_t re = 0, err = 0;
-  int hard = op == 3 ? tdiv<NC>(ws.data(), n, mode, ae, a, be, b, &re, r.data(), false, &err)
-                     : tsqrt<NC>(ws.data(), n, mode, ae, a, &re, r.data(), false, &err);
+  int hard = op == 3 ? tdiv<NC>(ws.data(), slab.data(), n, mode, ae, a, be, b, &re, r.data(), false, &err)
+                     : tsqrt<NC>(ws.data(), slab.data(), n, mode, ae, a, &re, r.data(), false, &err);
   if (hard) {
     std::fill(ws.begin(), ws.end(), 0x5A5A5A5Au);
-    const int again = op == 3 ? tdiv<NC>(ws.data(), n, mode, ae, a, be, b, &re, r.data(), true, &err)
-                              : tsqrt<NC>(ws.data(), n, mode, ae, a, &re, r.data(), true, &err);
+    const int again = op == 3 ? tdiv<NC>(ws.data(), slab.data(), n, mode, ae, a, be, b, &re, r.data(), true, &err)
+                              : tsqrt<NC>(ws.data(), slab.data(), n, mode, ae, a, &re, r.data(), true, &err);
     if (again) { printf("ERROR exact pass reported hard\n"); return; }
   }
   printf("%d %u %u", hard, err, re);
