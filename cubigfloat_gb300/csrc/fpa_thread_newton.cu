@@ -2,15 +2,18 @@
 // (configurations 18 and 19: up to 128 and up to 64 limbs).
 //
 // A CTA is one warp; each thread runs whole operations (tdiv / tsqrt of
-// fpa_thread_newton.cuh) in its columns of the warp's shared-memory workspace.  An
+// fpa_thread_newton.cuh) in its columns of the warp's shared-memory workspace and of the
+// CTA's operand slab.  Each thread first clears its workspace and slab columns, which sets
+// the zero guard limbs the product tiles rely on.  Warps take 32 operations at a time from
+// a counter, so a warp that shares its SM sub-partition with another takes fewer.  An
 // operation whose extra-limb quotient or root lies within the rounding margin needs the
 // exact correction, a full n x n product on one thread: done inline it would keep the other
 // 31 threads of its warp waiting, and with a few percent of such operations most warps
 // would carry one.  So the first pass only appends their indices to a list (one atomic per
 // warp) and writes nothing for them, and a second pass runs the listed operations again
-// with the exact correction, 32 at a time.  The list (4 bytes per operation) and the
-// operand slabs (one per CTA, fpa_thread_newton.cuh) are stream-ordered scratch from the
-// library's memory pool, so concurrent calls on different streams never share them.
+// with the exact correction, 32 at a time.  The counters, the list (4 bytes per operation)
+// and the slabs are stream-ordered scratch from the library's memory pool, so concurrent
+// calls on different streams never share them.
 #include <cuda_runtime.h>
 #include "fpa_thread_newton.cuh"
 #include "fpa_launch.h"
@@ -18,14 +21,15 @@
 namespace gfpa {
 
 template <int OP, int N>
-__global__ void __launch_bounds__(32) k_tnewton(ElementwiseArgs args, uint32_t *hard_count, uint32_t *hard_idx,
+__global__ void __launch_bounds__(32) k_tnewton(ElementwiseArgs args, uint32_t *ctl, uint32_t *hard_idx,
                                                 uint32_t *slabs, int pass) {
   extern __shared__ __align__(16) uint32_t smem[];
   const uint32_t lane = threadIdx.x;
   uint32_t *w = smem + lane;                          // this thread's columns
   uint32_t *slab = slabs + (size_t)blockIdx.x * 32 * TSpace<N>::slab + lane;
+  for (int j = 0; j < TSpace<N>::words; j++) w[TS * j] = 0u;
+  for (int j = 0; j < TSpace<N>::slab; j++) slab[TS * j] = 0u;
   const int n = (int)args.n;
-  const uint64_t total = (uint64_t)gridDim.x * 32;
   auto run = [&](uint64_t i, bool exact) -> int {
     const uint64_t off = i * (uint64_t)n;
     if (OP == OP_DIV)
@@ -35,20 +39,25 @@ __global__ void __launch_bounds__(32) k_tnewton(ElementwiseArgs args, uint32_t *
                     args.err);
   };
   if (pass == 0) {
-    const uint64_t iters = (args.count + total - 1) / total;
-    for (uint64_t it = 0; it < iters; it++) {         // the same trip count on every thread
-      const uint64_t i = it * total + (uint64_t)blockIdx.x * 32 + lane;
+    unsigned long long *next = reinterpret_cast<unsigned long long *>(ctl + 2);
+    for (;;) {                                        // the same trip count on every thread of the warp
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(next, 32ull);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base >= args.count) break;
+      const uint64_t i = base + lane;
       const int hard = (i < args.count) ? run(i, false) : 0;
       const uint32_t mask = __ballot_sync(0xFFFFFFFFu, hard != 0);
       if (mask) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(hard_count, (uint32_t)__popc(mask));
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (hard) hard_idx[base + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)i;
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(ctl, (uint32_t)__popc(mask));
+        b = __shfl_sync(0xFFFFFFFFu, b, 0);
+        if (hard) hard_idx[b + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)i;
       }
     }
   } else {
-    const uint64_t cnt = *hard_count;
+    const uint64_t total = (uint64_t)gridDim.x * 32;
+    const uint64_t cnt = *ctl;
     for (uint64_t j = (uint64_t)blockIdx.x * 32 + lane; j < cnt; j += total) run(hard_idx[j], true);
   }
 }
@@ -72,20 +81,21 @@ static cudaError_t launch_tnewton(const ElementwiseArgs &args, cudaStream_t stre
   if (grid == 0) return cudaSuccess;
   cudaMemPool_t pool;
   if (!gfpa_scratch_pool(&pool)) return cudaErrorMemoryAllocation;
-  // hard-operation list (count + 1 words), then one operand slab per CTA
-  const size_t list_bytes = ((size_t)(args.count + 1) * sizeof(uint32_t) + 255) & ~(size_t)255;
+  // control words (hard count, then the 64-bit operation counter), the hard-operation list
+  // (count words), then one operand slab per CTA
+  const size_t list_bytes = ((size_t)(args.count + 4) * sizeof(uint32_t) + 255) & ~(size_t)255;
   const size_t slab_bytes = (size_t)grid * 32 * TSpace<N>::slab * sizeof(uint32_t);
   uint32_t *list = nullptr;
   cudaError_t e = cudaMallocFromPoolAsync((void **)&list, list_bytes + slab_bytes, pool, stream);
   if (e != cudaSuccess) return e;
   uint32_t *slabs = list + list_bytes / sizeof(uint32_t);
-  e = cudaMemsetAsync(list, 0, sizeof(uint32_t), stream);
+  e = cudaMemsetAsync(list, 0, 4 * sizeof(uint32_t), stream);
   if (e == cudaSuccess) {
-    kern<<<grid, 32, smem, stream>>>(args, list, list + 1, slabs, 0);
+    kern<<<grid, 32, smem, stream>>>(args, list, list + 4, slabs, 0);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    kern<<<grid, 32, smem, stream>>>(args, list, list + 1, slabs, 1);
+    kern<<<grid, 32, smem, stream>>>(args, list, list + 4, slabs, 1);
     e = cudaGetLastError();
   }
   const cudaError_t ef = cudaFreeAsync(list, stream);

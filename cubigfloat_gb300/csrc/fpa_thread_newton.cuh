@@ -2,49 +2,63 @@
 //
 // The lane-group div/sqrt (op_div / op_sqrt in fpa_ops.cuh) spend most of their time outside
 // the limb products: staging operands, summing column blocks, syncing the group, and
-// products whose column blocks leave some lanes idle (a 66-limb operand is 17 blocks of 4).
-// Here every thread of a warp runs a whole operation of its own, so there is no cross-lane
-// traffic, no sync and no idle lane; the 32 operations of a warp share one limb count and
-// follow the same instruction stream.
+// products whose column blocks leave some lanes idle.  Here every thread of a warp runs a
+// whole operation of its own, so there is no cross-lane traffic, no sync and no idle lane;
+// the 32 operations of a warp share one limb count and follow the same instruction stream.
 //
-// The integer steps are those of op_div / op_sqrt, unchanged: the same Newton level
-// schedule (newton_levels, the one-thread small levels up to SMALL_LEVEL limbs), the same
-// truncations of every product and residual, the same Karp-Markstein last step with one
-// extra limb, the same 2^20-unit rounding margin and the same bounded exact correction.
-// The iterates, the extra-limb quotient / root and every result are therefore the same
-// integers, which the error analysis of those steps covers.  Only the data movement is
-// new: each product's limbs come out lowest first, 8 at a time (tmul), and go straight into
-// the step that uses them, so the full products are never stored.
+// The method is that of op_div / op_sqrt: a Newton iteration for the reciprocal (div) or the
+// reciprocal square root (sqrt) over levels 1 -> 2 -> 3 -> 5 -> ... -> h (the one-thread
+// register levels up to SMALL_LEVEL limbs first), then one Karp-Markstein step that yields
+// one limb more than the result, rounding decided from that extra limb when it lies at
+// least 2^20 units from a rounding boundary, and otherwise the bounded exact correction.
+// What differs is which limbs each product forms.  Every product here is restricted to the
+// limbs that its consumer reads, plus GUARD limbs below them: the low columns of
+// T = B_k' Y_k and of the Newton corrections, of q0 = A_top Y_h and of the final correction
+// D Y_h are never formed (a dropped carry changes a kept limb by at most one unit), and the
+// Karp-Markstein remainder D = A 2^96 - q0 B is a middle product of its dlen limbs, its
+// sign read from its top bit (|D| stays about 31 bits below 2^(32 dlen)).  The integer
+// steps are restated exactly by tests/test_km_error_bound.py, which checks that the
+// extra-limb quotient and root stay within a few units of the exact values at every size,
+// far inside the 2^20-unit margin; the exact correction is unchanged.  A 4096-bit division
+// forms about 12K limb products this way, against 21.8K with whole products.
 //
-// Storage: a thread's buffers live in its warp's shared-memory workspace with the warp's
-// 32 threads interleaved limb by limb (limb j of a buffer at p[32*j]), so the 32 threads
-// reading the same limb index touch 32 consecutive words.  Per thread, with N the largest
-// limb count served: regions R0 and R1 of N/2+8 limbs (Newton iterates, then the
-// Karp-Markstein remainder) and R3 of N+8 limbs (raw residual limbs, then the extra-limb
-// result with the half-size quotient / root placed at its final offset), 2N+24 words.
+// Products (tprod) are column-block product scans with an 8x8 register tile (96-bit
+// column sums fed by mac3), the tile loop unrolled twice so that the next tile's operands
+// load while the current one multiplies, and no bounds checks: every buffer a product reads
+// sits in zero guard limbs, so the tiles may read past either end (an operand read as the
+// product's second factor needs 8 zero limbs below it and zeros up to 8 limbs past its
+// length rounded up to 8; the first factor only the zeros above).
+//
+// Storage.  A thread's limb j of a buffer is at base[32*j] (the warp's 32 threads
+// interleaved limb by limb, so the 32 threads reading one limb index touch 32 consecutive
+// words).  Workspace (shared memory): three slots of N/2+8 limbs with zero guards, holding
+// the Newton iterates and residuals, then q0 / S0 and the remainder D.  Slab (global
+// memory, one per CTA, laid out the same way): B and A (div) or Xh = floor(A 2^(32-odd))
+// (sqrt), staged once per operation from the caller's natural layout so that every later
+// operand read is one coalesced warp load, and the extra-limb result Q' / S'.
 //
 // Operands a, b and the result r are the caller's arrays in the natural layout (number i's
-// limbs contiguous).  A thread reading its own number touches one 32-byte sector per limb
-// read across the warp's 32 numbers, and the products read the operands many times, so
-// each operation first copies its operands once into a slab in global memory laid out
-// like the workspace (limb j of this thread at slab[32*j]): A and B for div, Xh =
-// floor(A * 2^(32-odd)) for sqrt.  Every later operand read is then one coalesced 128-byte
-// warp load, and sqrt's shifted operand costs no shifts.  Reference semantics as op_div /
-// op_sqrt: fpa_warp_div.h:127-201, fpa_warp_sqrt.h:195-254.
+// limbs contiguous).  Reference semantics as op_div / op_sqrt: fpa_warp_div.h:127-201,
+// fpa_warp_sqrt.h:195-254.
 #pragma once
 #include "fpa_ops.cuh"
 
 namespace gfpa {
 
-constexpr int TS = 32;   // distance between a thread's consecutive limbs in the workspace
+constexpr int TS = 32;      // distance between a thread's consecutive limbs
+constexpr int GUARD = 2;    // limbs formed below the lowest limb a short product keeps
 
 template <int N>
 struct TSpace {
-  static constexpr int H = N / 2 + 8;        // R0, R1
-  static constexpr int Q = N + 8;            // R3
-  static constexpr int words = 2 * H + Q;    // per thread
-  static constexpr int slab = 2 * N + 8;     // operand slab words per thread (global memory)
-  static constexpr int min_limbs = 8;        // smaller numbers keep the lane-group path
+  static constexpr int SLOT = N / 2 + 8;                       // limbs per slot (multiple of 8)
+  // workspace (shared memory), in limbs: 8 readable + 8 zero | slot | 8 zero | slot | 8 zero |
+  // slot | 8 zero + 8 readable
+  static constexpr int Z0 = 16, Z1 = Z0 + SLOT + 8, Z2 = Z1 + SLOT + 8;
+  static constexpr int words = Z2 + SLOT + 16;
+  // slab (global memory), in limbs: 16 zero | B | 16 zero | A or Xh | 16 zero | Q' or S'
+  static constexpr int SB = 16, SA = SB + N + 16, SQ = SA + N + 16;
+  static constexpr int slab = SQ + N + 8;
+  static constexpr int min_limbs = 8;                          // smaller numbers keep the lane-group path
 };
 
 // Copies n limbs of a natural-layout number to a slab column (limb j at dst[TS*j]).
@@ -59,49 +73,48 @@ __device__ __forceinline__ void stage_limbs(uint32_t *dst, const uint32_t *src, 
   }
 }
 
-// ---- operand views: limb i of a number, 0 outside [0, len) ---------------------------
-struct VW {                     // a workspace buffer or a slab column
+// ---- operand views ------------------------------------------------------------------------
+struct PV {                     // a zero-guarded buffer: limb i at p[TS*i], read unchecked
+  const uint32_t *p;
+  __device__ __forceinline__ uint32_t get(int i) const { return p[TS * i]; }
+};
+struct VW {                     // any buffer: 0 outside [0, len)
   const uint32_t *p; int len;
   __device__ __forceinline__ uint32_t get(int i) const { return ((unsigned)i < (unsigned)len) ? p[TS * i] : 0u; }
 };
-// the Newton residual magnitude (ResidualMag) read from raw product limbs T[off ...] that
-// were stored from index 0: limb i is T[i] (or ~T[i] when the product was below 2^(32L)),
-// 0 at and above limb `lim` (= L - off) and outside [0, len)
-struct VResid {
-  const uint32_t *T; int lim, len; uint32_t neg;
-  __device__ __forceinline__ uint32_t get(int i) const {
-    if ((unsigned)i >= (unsigned)len || i >= lim) return 0u;
-    const uint32_t v = T[TS * i];
-    return neg ? v : ~v;
-  }
-};
 
-// ---- product: limbs of x * y lowest first, 8 at a time ----------------------------------
-// Column-block product scanning with an 8x8 register tile: output block cb gathers
-// x-block i times the y window y[8(cb-i)-8 .. 8(cb-i)+7] for every i with
-// 0 <= cb-i <= My (My = y's block count), into
-// 96-bit (lo, hi, top) column sums fed by mac3; the two limbs above a block carry into the
-// next one.  sink(cb, L) receives limbs 8cb .. 8cb+7 in L[0..7]; blocks stop once
-// `out_limbs` limbs have been produced (the higher limbs are not computed).
+__device__ __forceinline__ int rup8(int v) { return (v + 7) & ~7; }
+// first 8-limb output block of a product restricted to its limbs from `keep` up
+__device__ __forceinline__ int blk(int keep) { return max(0, keep - GUARD) >> 3; }
+// zeros from limb len of a slot up to 8 limbs past len rounded up (the rest is a zero guard)
+__device__ __forceinline__ void zero_tail(uint32_t *p, int len) {
+  const int e = rup8(len) + 8;
+  for (int i = len; i < e; i++) p[TS * i] = 0u;
+}
+
+// ---- product: output blocks [cb_lo, cb_hi) of x * y, 8 limbs at a time, lowest first -----
+// Output block cb gathers x-block i times the y window y[8(cb-i)-8 .. 8(cb-i)+7] for every i
+// with 0 <= cb-i <= My (My = y's block count), into 96-bit (lo, hi, top) column sums fed by
+// mac3; the two limbs above a block carry into the next one (none into block cb_lo).
+// sink(cb, L) receives limbs 8cb .. 8cb+7 in L[0..7].
 template <class X, class Y, class Sink>
-__device__ __forceinline__ void tmul(const X &x, int lx, const Y &y, int ly, int out_limbs, Sink &&sink) {
+__device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, int cb_lo, int cb_hi, Sink &&sink) {
   const int Mx = (lx + 7) >> 3, My = (ly + 7) >> 3;
-  const int Mo = min(Mx + My, (out_limbs + 7) >> 3);
+  const int Mo = min(Mx + My, cb_hi);
   uint32_t c0 = 0u, c1 = 0u;
 #pragma unroll 1
-  for (int cb = 0; cb < Mo; cb++) {
+  for (int cb = cb_lo; cb < Mo; cb++) {
     uint32_t lo[8], hi[8], tp[8];
 #pragma unroll
     for (int c = 0; c < 8; c++) { lo[c] = 0u; hi[c] = 0u; tp[c] = 0u; }
     lo[0] = c0; lo[1] = c1;
-    // the window spans y-blocks cb-i and cb-i-1, so x-block i reaches output blocks i .. i+My
     const int i0 = max(0, cb - My), i1 = min(cb, Mx - 1);
     uint32_t a[8], w[16];
 #pragma unroll
     for (int r = 0; r < 8; r++) a[r] = x.get(8 * i0 + r);
 #pragma unroll
     for (int m = 0; m < 16; m++) w[m] = y.get(8 * (cb - i0) - 8 + m);
-#pragma unroll 1
+#pragma unroll 2
     for (int i = i0; i <= i1; i++) {
       uint32_t an[8], wn[8];              // the next tile's operands, loaded ahead of the math
 #pragma unroll
@@ -124,7 +137,7 @@ __device__ __forceinline__ void tmul(const X &x, int lx, const Y &y, int ly, int
   }
 }
 
-// ---- rounding: X (workspace, xlen limbs) to n limbs, written to r (natural layout) -------
+// ---- rounding: X (xlen limbs, stride TS) to n limbs, written to r (natural layout) --------
 // X must have at least 32n+1 significant bits.  sticky_in: a nonzero part lies below X.
 // Returns X's bit length; ovf = 1 when rounding up carried into a new binade (the stored
 // mantissa is then 0.1000...).  Same decision as grp_round / store_limbs.
@@ -162,20 +175,20 @@ __device__ __forceinline__ int tround_store(const uint32_t *X, int xlen, int n, 
 // Returns 0 when the result is written, 1 when the extra-limb quotient lies within the
 // rounding margin and `exact` is false: the operation then needs the exact correction
 // (the caller runs it again with exact = true; nothing has been written).
+// w: this thread's workspace (zero-initialised guards); slab: its slab column.
 template <int N>
 __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp, const uint32_t *a, uint32_t b_exp,
                     const uint32_t *b, uint32_t *r_exp, uint32_t *r, bool exact, uint32_t *err) {
-  constexpr int H = TSpace<N>::H;
+  using S = TSpace<N>;
   const uint32_t act = c_action[3][classify(a_exp) * 9 + classify(b_exp)];
   if (act != ACT_DIV) { *r_exp = act; return 0; }
-  uint32_t *R0 = w, *R1 = w + TS * H, *R3 = w + TS * 2 * H;
-  uint32_t *SA = slab, *SB = slab + TS * n;          // A and B, limb j at [TS*j]
+  uint32_t *SA = slab + TS * S::SA, *SB = slab + TS * S::SB, *Q = slab + TS * S::SQ;
   stage_limbs(SA, a, n);
   stage_limbs(SB, b, n);
   int lv[24];
   const int nl = newton_levels(n, lv);
   const int l0 = small_levels_end(lv, nl, true);
-  uint32_t *Y = R0, *Y2 = R1;
+  uint32_t *Y = w + TS * S::Z0, *Y2 = w + TS * S::Z1, *E = w + TS * S::Z2;
   {
     const uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)SB[TS * (n - 1)];   // level 1: floor((2^64-1)/B_top)
     uint32_t v[SMALL_LEVEL + 1], bt[SMALL_LEVEL];
@@ -188,80 +201,89 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
     const int k = lv[l0 - 1];
 #pragma unroll
     for (int i = 0; i <= SMALL_LEVEL; i++) if (i <= k) Y[TS * i] = v[i];
+    zero_tail(Y, k + 1);
   }
   for (int li = l0; li < nl - 1; li++) {
     const int k = lv[li - 1], kp = lv[li], L = k + kp, lt = kp - k + 3;
-    // T = B_k' * Y_k: keep limbs k-1 .. L (the lower ones reach them only through carries)
-    tmul(VW{SB + TS * (n - kp), kp}, kp, VW{Y, k + 1}, k + 1, L + 1, [&](int cb, const uint32_t (&o)[10]) {
+    // T = B_k' Y_k ~ 2^(32L): E = its limbs k-1 .. kp+1, T[L] = 1 when T >= 2^(32L)
+    uint32_t tL = 0u;
+    tprod(PV{SB + TS * (n - kp)}, kp, PV{Y}, k + 1, blk(k - 1), L / 8 + 1, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         const int j = 8 * cb + q - (k - 1);
-        if (j >= 0 && j <= L - (k - 1)) R3[TS * j] = o[q];
+        if (j >= 0 && j < lt) E[TS * j] = o[q];
+        if (8 * cb + q == L) tL = o[q];
       }
     });
-    const uint32_t neg = R3[TS * (L - (k - 1))] != 0u;
-    // Y_k' = Y_k * 2^(32(k'-k)) +- M,  M = (Y_k * |E|) >> 32(k+1),  over k'+1 limbs
+    const bool neg = tL != 0u;
+    if (!neg)                                        // |2^(32L) - T| ~ complement (one unit low)
+      for (int j = 0; j < lt; j++) E[TS * j] = ~E[TS * j];
+    zero_tail(E, lt);
+    // Y_k' = Y_k 2^(32(k'-k)) +- M,  M = (Y_k |E|) >> 32(k+1),  over k'+1 limbs
     uint32_t cy = 0u;
     int next = 0;                                    // next limb of Y_k' to form
-    auto put = [&](int i, uint32_t m) {
+    auto put = [&](int i, uint32_t mv) {
       const uint32_t ys = (i >= kp - k) ? Y[TS * (i - (kp - k))] : 0u;
       uint32_t v;
-      if (neg) { v = ys - m - cy; cy = (ys < m || (ys == m && cy)) ? 1u : 0u; }
-      else { const uint64_t t = (uint64_t)ys + m + cy; v = (uint32_t)t; cy = (uint32_t)(t >> 32); }
+      if (neg) { v = ys - mv - cy; cy = (ys < mv || (ys == mv && cy)) ? 1u : 0u; }
+      else { const uint64_t t = (uint64_t)ys + mv + cy; v = (uint32_t)t; cy = (uint32_t)(t >> 32); }
       Y2[TS * i] = v;
     };
-    tmul(VW{Y, k + 1}, k + 1, VResid{R3, L - (k - 1), lt, neg}, lt, k + 1 + lt, [&](int cb, const uint32_t (&o)[10]) {
+    tprod(PV{Y}, k + 1, PV{E}, lt, blk(k + 1), (k + 1 + lt + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         const int i = 8 * cb + q - (k + 1);
-        if (i >= 0 && i < lt && i <= kp) { put(i, o[q]); next = i + 1; }
+        if (i >= 0 && i < lt) { put(i, o[q]); next = i + 1; }
       }
     });
     for (int i = next; i <= kp; i++) put(i, 0u);
+    zero_tail(Y2, kp + 1);
     uint32_t *t = Y; Y = Y2; Y2 = t;
   }
   // Karp-Markstein step with one limb more than the result (op_div): h = the last Newton
-  // level, m = n+2-h; q0 is placed at limb h-1 of R3 so that Q' forms in place.
+  // level, m = n+2-h.  q0 = floor(A_top Y / 2^(32(h+1))), A_top = the top m+1 limbs of A.
   const int h = lv[nl - 2], m = n + 2 - h;
-  uint32_t *D = Y2, *Q = R3;
-  tmul(VW{SA + TS * (n - m - 1), m + 1}, m + 1, VW{Y, h + 1}, h + 1, h + 2 + m, [&](int cb, const uint32_t (&o)[10]) {
+  uint32_t *q0 = E, *D = Y2;
+  tprod(PV{SA + TS * (n - m - 1)}, m + 1, PV{Y}, h + 1, blk(h + 1), (h + m + 9) / 8,
+        [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int j = 8 * cb + q - (h + 1);
-      if (j >= 0 && j <= m) Q[TS * (h - 1 + j)] = o[q];
-    }
-  });
-  // D = |A 2^96 - floor(q0 B / 2^(32(n-h-1)))| over n+4 limbs, its low m+2 limbs kept
-  const int dl = n + 4, dlen = m + 2, sh = n - h - 1;
+          for (int q = 0; q < 8; q++) {
+            const int j = 8 * cb + q - (h + 1);
+            if (j >= 0 && j <= m) q0[TS * j] = o[q];
+          }
+        });
+  zero_tail(q0, m + 1);
+  // D = A 2^96 - floor(q0 B / 2^(32(n-h-1))) mod 2^(32 dlen): the product's limbs sh .. sh+dlen-1
+  const int dlen = m + 2, sh = n - h - 1;
   uint32_t bw = 0u;
-  tmul(VW{Q + TS * (h - 1), m + 1}, m + 1, VW{SB, n}, n, n + m + 1, [&](int cb, const uint32_t (&o)[10]) {
+  tprod(PV{q0}, m + 1, PV{SB}, n, blk(sh), (sh + dlen + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q - sh;
-      if (i >= 0 && i < dl) {
-        const uint32_t xa = (i >= 3 && i - 3 < n) ? SA[TS * (i - 3)] : 0u, xq = o[q];
-        const uint32_t v = xa - xq - bw;
+      if (i >= 0 && i < dlen) {
+        const uint32_t xa = i >= 3 ? SA[TS * (i - 3)] : 0u, xq = o[q];
+        D[TS * i] = xa - xq - bw;
         bw = (xa < xq || (xa == xq && bw)) ? 1u : 0u;
-        if (i < dlen) D[TS * i] = v;
       }
     }
   });
-  const bool dneg = bw != 0u;
+  const bool dneg = (D[TS * (dlen - 1)] >> 31) != 0u;
   if (dneg) {                                        // D = -D (mod 2^(32 dlen))
     uint32_t c = 1u;
     for (int i = 0; i < dlen; i++) { const uint32_t v = ~D[TS * i] + c; c = (c && v == 0u) ? 1u : 0u; D[TS * i] = v; }
   }
-  // Q' = q0 2^(32(h-1)) +- floor(D Y / 2^(32(h+2))),  n+2 limbs
+  zero_tail(D, dlen);
+  // Q' = q0 2^(32(h-1)) +- floor(D Y / 2^(32(h+2))),  n+2 limbs, into the slab
   uint32_t cq = 0u;
   int nextq = 0;
   auto putq = [&](int i, uint32_t c) {
-    const uint32_t qv = (i >= h - 1) ? Q[TS * i] : 0u;
+    const uint32_t qv = (i >= h - 1) ? q0[TS * (i - (h - 1))] : 0u;
     uint32_t v;
     if (dneg) { v = qv - c - cq; cq = (qv < c || (qv == c && cq)) ? 1u : 0u; }
     else { const uint64_t t = (uint64_t)qv + c + cq; v = (uint32_t)t; cq = (uint32_t)(t >> 32); }
     Q[TS * i] = v;
   };
-  tmul(VW{D, dlen}, dlen, VW{Y, h + 1}, h + 1, dlen + h + 1, [&](int cb, const uint32_t (&o)[10]) {
+  tprod(PV{D}, dlen, PV{Y}, h + 1, blk(h + 2), (dlen + h + 8) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q - (h + 2);
@@ -284,13 +306,14 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
     }
   }
   if (!exact) return 1;
-  // exact correction: Q = floor(Q'/2^32) (n+1 limbs, at limb 1 of R3),
-  // Rm = (A 2^(32n) - Q B) mod 2^(32(n+2)) over R0..R1
-  uint32_t *Qc = Q + TS, *Rm = R0;
+  // exact correction: Qc = floor(Q'/2^32) (n+1 limbs, from limb 1 of Q'),
+  // Rm = (A 2^(32n) - Qc B) mod 2^(32(n+2)) over slots 0 and 1 (their guard limbs between
+  // them are cleared again at the end)
+  uint32_t *Qc = Q + TS, *Rm = w + TS * S::Z0;
   const uint32_t qt = Qc[TS * n];
   uint32_t c1 = 0u, b2 = 0u;
   auto putr = [&](int i, uint32_t p) {
-    // P2 = Q[0..n) B + (qt B) 2^(32n): add the small multiple, then subtract from A 2^(32n)
+    // P2 = Qc[0..n) B + (qt B) 2^(32n): add the small multiple, then subtract from A 2^(32n)
     uint32_t smv = 0u;                               // (qt B) 2^(32n), qt in {0, 1, 2, 4}
     if (i >= n && qt) {
       const int t = i - n;
@@ -306,7 +329,7 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
     Rm[TS * i] = v;
   };
   int nextr = 0;
-  tmul(VW{Qc, n}, n, VW{SB, n}, n, n + 2, [&](int cb, const uint32_t (&o)[10]) {
+  tprod(VW{Qc, n}, n, VW{SB, n}, n, 0, (n + 2 + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q;
@@ -314,7 +337,7 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
     }
   });
   for (int i = nextr; i < n + 2; i++) putr(i, 0u);
-  // 0 <= Rm < B, Q stepped alongside (bounded; a hit bound sets the error word)
+  // 0 <= Rm < B, Qc stepped alongside (bounded; a hit bound sets the error word)
   int guard = 0;
   while ((Rm[TS * (n + 1)] >> 31) != 0u && guard < 64) {
     uint32_t bq = 1u;
@@ -352,9 +375,10 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
     nz |= Rm[TS * i];
     if (c2 == 0 && x != y) c2 = x > y ? 1 : -1;
   }
+  for (int i = S::SLOT; i < S::SLOT + 8; i++) Rm[TS * i] = 0u;   // the guard limbs between slots 0 and 1
   const uint32_t rb = c2 >= 0 ? 1u : 0u, sticky = (nz != 0u && c2 != 0) ? 1u : 0u;
-  // X = 2Q + rb, n+2 limbs, formed in place one limb below Q (limb i of X over limb i of R3)
-  uint32_t *X = R3;
+  // X = 2Qc + rb, n+2 limbs, formed in place one limb below Qc (limb i of X over limb i of Q')
+  uint32_t *X = Q;
   for (int i = 0; i < n + 2; i++) {
     const uint32_t qi = i <= n ? Qc[TS * i] : 0u, qm = i > 0 ? Qc[TS * (i - 1)] : 0u;
     X[TS * i] = (qi << 1) | (i > 0 ? (qm >> 31) : rb);
@@ -370,35 +394,34 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
 
 // ---- sqrt --------------------------------------------------------------------------------
 // Same return convention as tdiv.  Steps of op_sqrt: A_ext = A 2^(32n - odd), Xh = its top
-// n+1 limbs (read from A on the fly), Newton on 1/sqrt with three products per level, the
-// Karp-Markstein step with one limb more, the exact correction with R = A_ext - S^2.
+// n+1 limbs, Newton on 1/sqrt with three products per level, the Karp-Markstein step with
+// one limb more, the exact correction with R = A_ext - S^2.
 template <int N>
 __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp, const uint32_t *a, uint32_t *r_exp,
                      uint32_t *r, bool exact, uint32_t *err) {
-  constexpr int H = TSpace<N>::H;
+  using S = TSpace<N>;
   const uint32_t act = c_sqrt_action[classify(a_exp)];
   if (act != ACT_SQRT) { *r_exp = act; return 0; }
-  uint32_t *R0 = w, *R1 = w + TS * H, *R3 = w + TS * 2 * H;
   const long long e = (long long)(a_exp >> 1) - BIAS;
   const int odd = (int)(e & 1);
   const long long eh = (e + odd) / 2;
+  uint32_t *X = slab + TS * S::SA, *Sq = slab + TS * S::SQ;
   // Xh = floor(A * 2^(32 - odd)), n+1 limbs, staged in the slab
   {
     uint32_t prev = 0u;
     for (int j = 0; j < n; j++) {
       const uint32_t cur = a[j];
-      slab[TS * j] = odd ? ((prev >> 1) | (cur << 31)) : prev;
+      X[TS * j] = odd ? ((prev >> 1) | (cur << 31)) : prev;
       prev = cur;
     }
-    slab[TS * n] = odd ? (prev >> 1) : prev;
+    X[TS * n] = odd ? (prev >> 1) : prev;
   }
-  const VW xh{slab, n + 1};
   int lv[24];
   const int nl = newton_levels(n, lv);
   const int l0 = small_levels_end(lv, nl, true);
-  uint32_t *Z = R0, *Z2 = R1;
+  uint32_t *Z = w + TS * S::Z0, *Z2 = w + TS * S::Z1, *E = w + TS * S::Z2;
   {
-    const uint64_t x1 = (uint64_t)xh.get(n) << 32;
+    const uint64_t x1 = (uint64_t)X[TS * n] << 32;
     const uint64_t s1 = isqrt64(x1);
     const uint64_t z = 0xFFFFFFFFFFFFFFFFull / s1;
     uint32_t v[SMALL_LEVEL + 1], xt[SMALL_LEVEL];
@@ -406,48 +429,53 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
     for (int i = 0; i <= SMALL_LEVEL; i++) v[i] = 0u;
     v[0] = (uint32_t)z; v[1] = (uint32_t)(z >> 32);
 #pragma unroll
-    for (int i = 0; i < SMALL_LEVEL; i++) xt[i] = xh.get(n + 1 - SMALL_LEVEL + i);
+    for (int i = 0; i < SMALL_LEVEL; i++) xt[i] = (n + 1 - SMALL_LEVEL + i >= 0) ? X[TS * (n + 1 - SMALL_LEVEL + i)] : 0u;
     small_levels<true>(xt, lv, l0, v);
     const int k = lv[l0 - 1];
 #pragma unroll
     for (int i = 0; i <= SMALL_LEVEL; i++) if (i <= k) Z[TS * i] = v[i];
+    zero_tail(Z, k + 1);
   }
-  constexpr int WOFF = N / 2 + 4;                    // Wraw at R3 + WOFF (V1s below it)
   for (int li = l0; li < nl - 1; li++) {
     const int k = lv[li - 1], kp = lv[li];
-    const int j = k > 2 ? k - 2 : 0, l1 = kp + k + 1 - j, L = kp + 2 * k - j, lt = kp - k + 3;
-    uint32_t *V1s = R3, *Wr = R3 + TS * WOFF;
-    // V1 = X_k' Z_k, kept from limb j up
-    tmul(VW{slab + TS * (n + 1 - kp), kp}, kp, VW{Z, k + 1}, k + 1, kp + k + 1, [&](int cb, const uint32_t (&o)[10]) {
+    const int j = k > 2 ? k - 2 : 0, l1 = kp + k + 1 - j, L = kp + 2 * k - j, lt = kp - k + 3, off = 2 * k - 1 - j;
+    uint32_t *V1s = Z2;
+    // V1 = X_k' Z_k, its limbs j .. j+l1-1
+    tprod(PV{X + TS * (n + 1 - kp)}, kp, PV{Z}, k + 1, blk(j), (j + l1 + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         const int i = 8 * cb + q - j;
         if (i >= 0 && i < l1) V1s[TS * i] = o[q];
       }
     });
-    // W = (V1 >> 32j) Z_k, kept from limb 2k-1-j to L
-    const int off = 2 * k - 1 - j;
-    tmul(VW{V1s, l1}, l1, VW{Z, k + 1}, k + 1, L + 1, [&](int cb, const uint32_t (&o)[10]) {
+    zero_tail(V1s, l1);
+    // W = (V1 >> 32j) Z_k ~ 2^(32L): E = its limbs off .. off+lt-1, W[L] = 1 when W >= 2^(32L)
+    uint32_t wL = 0u;
+    tprod(PV{V1s}, l1, PV{Z}, k + 1, blk(off), L / 8 + 1, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         const int i = 8 * cb + q - off;
-        if (i >= 0 && i <= L - off) Wr[TS * i] = o[q];
+        if (i >= 0 && i < lt) E[TS * i] = o[q];
+        if (8 * cb + q == L) wL = o[q];
       }
     });
-    const uint32_t neg = Wr[TS * (L - off)] != 0u;
-    // Z_k' = Z_k 2^(32(k'-k)) +- M,  M = (Z_k |E|) >> (32(k+1)+1),  over k'+1 limbs
+    const bool neg = wL != 0u;
+    if (!neg)
+      for (int i = 0; i < lt; i++) E[TS * i] = ~E[TS * i];
+    zero_tail(E, lt);
+    // Z_k' = Z_k 2^(32(k'-k)) +- M,  M = (Z_k |E|) >> (32(k+1)+1),  over k'+1 limbs (into V1s' slot)
     uint32_t cy = 0u, prev = 0u;
     int next = 0;
-    auto put = [&](int i, uint32_t m) {
+    auto put = [&](int i, uint32_t mv) {
       const uint32_t zs = (i >= kp - k) ? Z[TS * (i - (kp - k))] : 0u;
       uint32_t v;
-      if (neg) { v = zs - m - cy; cy = (zs < m || (zs == m && cy)) ? 1u : 0u; }
-      else { const uint64_t t = (uint64_t)zs + m + cy; v = (uint32_t)t; cy = (uint32_t)(t >> 32); }
+      if (neg) { v = zs - mv - cy; cy = (zs < mv || (zs == mv && cy)) ? 1u : 0u; }
+      else { const uint64_t t = (uint64_t)zs + mv + cy; v = (uint32_t)t; cy = (uint32_t)(t >> 32); }
       Z2[TS * i] = v;
     };
     // M[i] = (P[k+1+i] >> 1) | (P[k+2+i] << 31): formed when P[k+2+i] arrives (the limbs of
     // the last block past the product's end are 0)
-    tmul(VW{Z, k + 1}, k + 1, VResid{Wr, L - off, lt, neg}, lt, k + 1 + lt, [&](int cb, const uint32_t (&o)[10]) {
+    tprod(PV{Z}, k + 1, PV{E}, lt, blk(k + 1), 1 << 20, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
       for (int q = 0; q < 8; q++) {
         const int i = 8 * cb + q - (k + 2);
@@ -456,55 +484,55 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
       }
     });
     for (int i = next; i <= kp; i++) put(i, i == next ? (prev >> 1) : 0u);
+    zero_tail(Z2, kp + 1);
     uint32_t *t = Z; Z = Z2; Z2 = t;
   }
-  // Karp-Markstein with one limb more (op_sqrt): S0 = floor(Xt Z / 2^(32(h+1))), placed at
-  // limb h-1 of R3 so that S' forms in place
+  // Karp-Markstein with one limb more (op_sqrt): S0 = floor(Xt Z / 2^(32(h+1))),
+  // Xt = the top m+1 limbs of Xh
   const int h = lv[nl - 2], m = n + 2 - h;
-  uint32_t *D = Z2, *S = R3;
-  tmul(VW{slab + TS * (n - m), m + 1}, m + 1, VW{Z, h + 1}, h + 1, h + 2 + m, [&](int cb, const uint32_t (&o)[10]) {
+  uint32_t *S0 = E, *D = Z2;
+  tprod(PV{X + TS * (n - m)}, m + 1, PV{Z}, h + 1, blk(h + 1), (h + m + 9) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q - (h + 1);
-      if (i >= 0 && i <= m) S[TS * (h - 1 + i)] = o[q];
+      if (i >= 0 && i <= m) S0[TS * i] = o[q];
     }
   });
-  // D = |Xh 2^96 - S0^2 2^(32(2h-n))| over n+6 limbs, its low m+3 limbs kept
-  const int dl = n + 6, dlen = m + 3, ssh = 2 * h - n;
+  zero_tail(S0, m + 1);
+  // D = Xh 2^96 - S0^2 2^(32(2h-n)) mod 2^(32 dlen): the square's limbs below dlen - ssh
+  const int dlen = m + 3, ssh = 2 * h - n;
   uint32_t bw = 0u;
   auto putd = [&](int i, uint32_t ss) {
-    const uint32_t xs = xh.get(i - 3);
-    const uint32_t v = xs - ss - bw;
+    const uint32_t xs = i >= 3 ? X[TS * (i - 3)] : 0u;
+    D[TS * i] = xs - ss - bw;
     bw = (xs < ss || (xs == ss && bw)) ? 1u : 0u;
-    if (i < dlen) D[TS * i] = v;
   };
-  for (int i = 0; i < ssh && i < dl; i++) putd(i, 0u);
-  const VW s0{S + TS * (h - 1), m + 1};
-  tmul(s0, m + 1, s0, m + 1, 2 * m + 2, [&](int cb, const uint32_t (&o)[10]) {
+  for (int i = 0; i < ssh; i++) putd(i, 0u);
+  tprod(PV{S0}, m + 1, PV{S0}, m + 1, 0, (dlen - ssh + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q + ssh;
-      if (i < dl && 8 * cb + q < 2 * m + 2) putd(i, o[q]);
+      if (i < dlen) putd(i, o[q]);
     }
   });
-  for (int i = 2 * m + 2 + ssh; i < dl; i++) putd(i, 0u);
-  const bool dneg = bw != 0u;
+  const bool dneg = (D[TS * (dlen - 1)] >> 31) != 0u;
   if (dneg) {
     uint32_t c = 1u;
     for (int i = 0; i < dlen; i++) { const uint32_t v = ~D[TS * i] + c; c = (c && v == 0u) ? 1u : 0u; D[TS * i] = v; }
   }
-  // S' = S0 2^(32(h-1)) +- floor(D Z / 2^(32(h+3)+1)),  n+2 limbs
+  zero_tail(D, dlen);
+  // S' = S0 2^(32(h-1)) +- floor(D Z / 2^(32(h+3)+1)),  n+2 limbs, into the slab
   uint32_t cs = 0u, prev = 0u;
   int nexts = 0;
   auto puts = [&](int i, uint32_t c) {
-    const uint32_t sv = (i >= h - 1) ? S[TS * i] : 0u;
+    const uint32_t sv = (i >= h - 1) ? S0[TS * (i - (h - 1))] : 0u;
     uint32_t v;
     if (dneg) { v = sv - c - cs; cs = (sv < c || (sv == c && cs)) ? 1u : 0u; }
     else { const uint64_t t = (uint64_t)sv + c + cs; v = (uint32_t)t; cs = (uint32_t)(t >> 32); }
-    S[TS * i] = v;
+    Sq[TS * i] = v;
   };
   const int plen = dlen + h + 1;
-  tmul(VW{D, dlen}, dlen, VW{Z, h + 1}, h + 1, plen, [&](int cb, const uint32_t (&o)[10]) {
+  tprod(PV{D}, dlen, PV{Z}, h + 1, blk(h + 3), 1 << 20, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int pj = 8 * cb + q;
@@ -515,26 +543,28 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
       }
     }
   });
-  for (int i = nexts; i < n + 2; i++) {              // V1 limbs past its end are 0
+  for (int i = nexts; i < n + 2; i++) {              // product limbs past its end are 0
     const int pj = i + h + 4;
     puts(i, pj == plen ? (prev >> 1) : 0u);
   }
   {
-    const uint32_t u = S[0] & 0x7FFFFFFFu;
-    if (S[TS * (n + 1)] == 0u && u >= (1u << 20) && u <= 0x7FFFFFFFu - (1u << 20)) {
+    const uint32_t u = Sq[0] & 0x7FFFFFFFu;
+    if (Sq[TS * (n + 1)] == 0u && u >= (1u << 20) && u <= 0x7FFFFFFFu - (1u << 20)) {
       int ovf;
-      const int Lb = tround_store(S, n + 1, n, 1u, mode, 0u, r, ovf);
+      const int Lb = tround_store(Sq, n + 1, n, 1u, mode, 0u, r, ovf);
       *r_exp = exp_word(eh - 32LL * n - 32 + Lb + ovf, 0u);
       return 0;
     }
   }
   if (!exact) return 1;
-  // exact correction: S = floor(S'/2^32) (n+1 limbs), Rm = (A_ext - S^2) mod 2^(32(n+2))
-  uint32_t *Sc = S + TS, *Rm = R0;
+  // exact correction: Sc = floor(S'/2^32) (n+1 limbs), Rm = (A_ext - Sc^2) mod 2^(32(n+2))
+  // over slots 0 and 1
+  uint32_t *Sc = Sq + TS, *Rm = w + TS * S::Z0;
+  const VW xh{X, n + 1};
   const uint32_t stop = Sc[TS * n];
   uint32_t c1 = 0u, b2 = 0u;
   auto putr = [&](int i, uint32_t p) {
-    uint32_t smv = 0u;                               // (2 stop S) 2^(32n)
+    uint32_t smv = 0u;                               // (2 stop Sc) 2^(32n)
     if (i >= n && stop) {
       const int t = i - n;
       const uint32_t v = (t < n) ? Sc[TS * t] : 0u, wv = (t >= 1 && t - 1 < n) ? Sc[TS * (t - 1)] : 0u;
@@ -550,7 +580,7 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
   };
   int nextr = 0;
   const VW sl{Sc, n};
-  tmul(sl, n, sl, n, n + 2, [&](int cb, const uint32_t (&o)[10]) {
+  tprod(sl, n, sl, n, 0, (n + 2 + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q;
@@ -558,9 +588,9 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
     }
   });
   for (int i = nextr; i < n + 2; i++) putr(i, 0u);
-  // 0 <= Rm <= 2S, S stepped alongside (bounded; a hit bound sets the error word)
+  // 0 <= Rm <= 2Sc, Sc stepped alongside (bounded; a hit bound sets the error word)
   int guard = 0;
-  while ((Rm[TS * (n + 1)] >> 31) != 0u && guard < 64) {            // Rm += 2S - 1, S -= 1
+  while ((Rm[TS * (n + 1)] >> 31) != 0u && guard < 64) {            // Rm += 2Sc - 1, Sc -= 1
     uint32_t c = 0u;
     for (int i = 0; i < n + 2; i++) {
       const uint32_t v = (i <= n ? Sc[TS * i] : 0u), wv = (i >= 1 && i - 1 <= n) ? Sc[TS * (i - 1)] : 0u;
@@ -574,7 +604,7 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
     for (int i = 0; i <= n && bq; i++) { const uint32_t v = Sc[TS * i]; Sc[TS * i] = v - 1u; bq = v == 0u; }
     guard++;
   }
-  for (;;) {                                          // Rm -= 2S + 1, S += 1 while Rm > 2S
+  for (;;) {                                          // Rm -= 2Sc + 1, Sc += 1 while Rm > 2Sc
     int cmp = 0;
     for (int i = n + 1; i >= 0 && cmp == 0; i--) {
       const uint32_t v = (i <= n ? Sc[TS * i] : 0u), wv = (i >= 1 && i - 1 <= n) ? Sc[TS * (i - 1)] : 0u;
@@ -594,7 +624,7 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
     guard++;
   }
   if (guard >= 64) atomicOr(err, 2u);
-  // round bit: Rm > S;  sticky: Rm != 0
+  // round bit: Rm > Sc;  sticky: Rm != 0
   int c2 = 0;
   uint32_t nz = 0u;
   for (int i = n + 1; i >= 0; i--) {
@@ -602,14 +632,15 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
     nz |= x;
     if (c2 == 0 && x != y) c2 = x > y ? 1 : -1;
   }
+  for (int i = S::SLOT; i < S::SLOT + 8; i++) Rm[TS * i] = 0u;   // the guard limbs between slots 0 and 1
   const uint32_t rb = c2 > 0 ? 1u : 0u, sticky = nz != 0u ? 1u : 0u;
-  uint32_t *X = R3;                                   // 2S + rb in place one limb below S
+  uint32_t *Xr = Sq;                                  // 2Sc + rb in place one limb below Sc
   for (int i = 0; i < n + 2; i++) {
     const uint32_t si = i <= n ? Sc[TS * i] : 0u, sm = i > 0 ? Sc[TS * (i - 1)] : 0u;
-    X[TS * i] = (si << 1) | (i > 0 ? (sm >> 31) : rb);
+    Xr[TS * i] = (si << 1) | (i > 0 ? (sm >> 31) : rb);
   }
   int ovf;
-  const int Lb = tround_store(X, n + 2, n, sticky, mode, 0u, r, ovf);
+  const int Lb = tround_store(Xr, n + 2, n, sticky, mode, 0u, r, ovf);
   *r_exp = exp_word(eh - 32LL * n - 1 + Lb + ovf, 0u);
   return 0;
 }

@@ -1,5 +1,5 @@
 """The one-thread-per-operation div and sqrt (tdiv / tsqrt in
-cubigfloat_gb300/csrc/fpa_thread_newton.cuh, with tmul, tround_store and the Newton
+cubigfloat_gb300/csrc/fpa_thread_newton.cuh, with tprod, tround_store and the Newton
 building blocks of fpa_ops.cuh under them), compiled for the host from the device source,
 bit-exact against the oracle in every rounding mode, at 8 to 128 limbs, on random operands,
 the reference generator's limb pattern, near-exact quotients and squares, all-ones
@@ -48,13 +48,14 @@ using namespace gfpa;
 // one operation per input line: op n mode a_exp a[0..n) [b_exp b[0..n)]
 template <int NC>
 static void run(int op, int n, int mode, uint32_t ae, const uint32_t *a, uint32_t be, const uint32_t *b) {
-  std::vector<uint32_t> ws((size_t)32 * TSpace<NC>::words + 64, 0xA5A5A5A5u), r(n, 0);
-  std::vector<uint32_t> slab((size_t)32 * TSpace<NC>::slab + 64, 0xC3C3C3C3u);
+  // one thread's workspace and slab columns, cleared once and reused by every operation, as
+  // a kernel thread does
+  static std::vector<uint32_t> ws((size_t)32 * TSpace<NC>::words, 0u), slab((size_t)32 * TSpace<NC>::slab, 0u);
+  std::vector<uint32_t> r(n, 0);
   uint32_t re = 0, err = 0;
   int hard = op == 3 ? tdiv<NC>(ws.data(), slab.data(), n, mode, ae, a, be, b, &re, r.data(), false, &err)
                      : tsqrt<NC>(ws.data(), slab.data(), n, mode, ae, a, &re, r.data(), false, &err);
   if (hard) {
-    std::fill(ws.begin(), ws.end(), 0x5A5A5A5Au);
     const int again = op == 3 ? tdiv<NC>(ws.data(), slab.data(), n, mode, ae, a, be, b, &re, r.data(), true, &err)
                               : tsqrt<NC>(ws.data(), slab.data(), n, mode, ae, a, &re, r.data(), true, &err);
     if (again) { printf("ERROR exact pass reported hard\n"); return; }
@@ -111,7 +112,7 @@ def host_source():
     body = re.sub(r"__device__\s+__forceinline__", "inline", body)
     body = re.sub(r"__device__\s+__noinline__", "", body)
     body = re.sub(r"__device__", "", body)
-    body = body.replace("#pragma unroll 1", "").replace("#pragma unroll", "")
+    body = re.sub(r"#pragma unroll[^\n]*", "", body)
     return SHIMS + body + MAIN
 
 

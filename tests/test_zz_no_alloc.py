@@ -88,3 +88,5 @@ def test_noalloc_rejects_more_than_its_maximum():
     rc = L.fpa_batch_run_noalloc(d.ctypes.data_as(ctypes.c_void_p), len(descs), None, None, None, None, None,
                                  None, None)
     assert rc == fpa.fpa_invalid_counts
+    # the rejected call touched nothing: the error word of the last batch is still readable and clear
+    assert L.fpa_batch_noalloc_errors(None) == 0
