@@ -34,7 +34,7 @@ struct ElementwiseArgs {
 // per lane), which the autotuner can choose (mostly for div/sqrt); 16 to 19 are elementwise
 // only: 16 runs add/sub and mul, one thread per operation on shared-memory rows for 8, 16
 // and 32 limbs and lane groups otherwise; 17 runs add/sub on four lanes x 16 limbs in
-// registers (fpa_addsub_narrow.cu); 18 and 19 run div and sqrt with one thread per
+// registers (fpa_addsub_narrow.cu); 18 and 19 run mul, div and sqrt with one thread per
 // operation and 8x8-limb product tiles, up to 128 and 64 limbs (fpa_thread_newton.cu).
 static const int gfpa_cfg_G[GFPA_NUM_CFGS] = {4, 8, 8, 16, 32, 32, 32, 16, 8, 16, 8, 8, 16, 8, 16, 4, 4, 4, 1, 1};
 static const int gfpa_cfg_K[GFPA_NUM_CFGS] = {2, 2, 4, 4, 4, 8, 16, 8, 16, 16, 4, 4, 4, 8, 8, 4, 8, 16, 8, 8};
@@ -43,7 +43,7 @@ static inline int gfpa_cfg_capacity(int c) { return gfpa_cfg_G[c] * gfpa_cfg_K[c
 // configurations 16 to 19 have elementwise kernels only
 static inline bool gfpa_cfg_elementwise_only(int c) { return c >= 16; }
 static inline bool gfpa_cfg_supports(int c, int op) {
-  if (c >= 18) return op == 3 || op == 4;
+  if (c >= 18) return op == 2 || op == 3 || op == 4;
   return c < 16 || op <= 1 || (c == 16 && op == 2);
 }
 // the current device's memory pool for stream-ordered scratch (fpa_api.cu)

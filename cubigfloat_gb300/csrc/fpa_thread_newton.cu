@@ -1,4 +1,4 @@
-// fpa_thread_newton.cu -- elementwise div and sqrt with one thread per operation
+// fpa_thread_newton.cu -- elementwise mul, div and sqrt with one thread per operation
 // (configurations 18 and 19: up to 128 and up to 64 limbs).
 //
 // A CTA is one warp; each thread runs whole operations (tdiv / tsqrt of
@@ -102,6 +102,97 @@ static cudaError_t launch_tnewton(const ElementwiseArgs &args, cudaStream_t stre
   return e != cudaSuccess ? e : ef;
 }
 
+// mul (tmul_op): A in this thread's shared-memory columns (read as the product's first
+// factor: 8 limbs per tile), B and the product limbs that feed the rounding in its slab
+// column.  Measured on GB300 at 4096 bits: A and B both in shared memory allow 5 warps per
+// SM (3.88 ms per 2^20 operations), both in the slab leave the operand reads to L2
+// (3.10 ms); this split holds 11 warps per SM (2.37 ms).  Limb offsets per thread:
+template <int N>
+struct MSpace {
+  static constexpr int words = N + 16;                  // shared memory: A, then zeros
+  static constexpr int SB = 16, GQ = N + 32;            // slab: 16 zero | B | 16 zero | Q
+  static constexpr int slab = GQ + N + 8;
+};
+
+template <int N>
+__global__ void __launch_bounds__(32) k_tmul(ElementwiseArgs args, uint32_t *ctl, uint32_t *hard_idx, uint32_t *slabs,
+                                             int pass) {
+  using S = MSpace<N>;
+  extern __shared__ __align__(16) uint32_t smem[];
+  const uint32_t lane = threadIdx.x;
+  uint32_t *A = smem + lane;
+  uint32_t *slab = slabs + (size_t)blockIdx.x * 32 * S::slab + lane;
+  for (int j = 0; j < S::words; j++) A[TS * j] = 0u;
+  for (int j = 0; j < S::slab; j++) slab[TS * j] = 0u;
+  uint32_t *B = slab + TS * S::SB, *Q = slab + TS * S::GQ;
+  const int n = (int)args.n;
+  auto run = [&](uint64_t i, bool exact) -> int {
+    const uint64_t off = i * (uint64_t)n;
+    return tmul_op(A, B, Q, n, args.mode, args.a_exps[i], args.a_limbs + off, args.b_exps[i], args.b_limbs + off,
+                   args.r_exps + i, args.r_limbs + off, exact);
+  };
+  if (pass == 0) {
+    unsigned long long *next = reinterpret_cast<unsigned long long *>(ctl + 2);
+    for (;;) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(next, 32ull);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base >= args.count) break;
+      const uint64_t i = base + lane;
+      const int hard = (i < args.count) ? run(i, false) : 0;
+      const uint32_t mask = __ballot_sync(0xFFFFFFFFu, hard != 0);
+      if (mask) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(ctl, (uint32_t)__popc(mask));
+        b = __shfl_sync(0xFFFFFFFFu, b, 0);
+        if (hard) hard_idx[b + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)i;
+      }
+    }
+  } else {
+    const uint64_t total = (uint64_t)gridDim.x * 32;
+    const uint64_t cnt = *ctl;
+    for (uint64_t j = (uint64_t)blockIdx.x * 32 + lane; j < cnt; j += total) run(hard_idx[j], true);
+  }
+}
+
+template <int N>
+static cudaError_t launch_tmul(const ElementwiseArgs &args, cudaStream_t stream, int sms) {
+  using S = MSpace<N>;
+  constexpr size_t smem = (size_t)32 * S::words * sizeof(uint32_t);
+  auto kern = k_tmul<N>;
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int blocks = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, 32, smem);
+    if (e != cudaSuccess) return e;
+    per_sm = blocks > 0 ? blocks : 1;
+  }
+  const uint64_t need = (args.count + 31) / 32, cap = (uint64_t)sms * (uint64_t)per_sm;
+  const unsigned grid = (unsigned)(need < cap ? need : cap);
+  if (grid == 0) return cudaSuccess;
+  cudaMemPool_t pool;
+  if (!gfpa_scratch_pool(&pool)) return cudaErrorMemoryAllocation;
+  const size_t list_bytes = ((size_t)(args.count + 4) * sizeof(uint32_t) + 255) & ~(size_t)255;
+  const size_t slab_bytes = (size_t)grid * 32 * S::slab * sizeof(uint32_t);
+  uint32_t *list = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync((void **)&list, list_bytes + slab_bytes, pool, stream);
+  if (e != cudaSuccess) return e;
+  uint32_t *slabs = list + list_bytes / sizeof(uint32_t);
+  e = cudaMemsetAsync(list, 0, 4 * sizeof(uint32_t), stream);
+  if (e == cudaSuccess) {
+    kern<<<grid, 32, smem, stream>>>(args, list, list + 4, slabs, 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
+    kern<<<grid, 32, smem, stream>>>(args, list, list + 4, slabs, 1);
+    e = cudaGetLastError();
+  }
+  const cudaError_t ef = cudaFreeAsync(list, stream);
+  return e != cudaSuccess ? e : ef;
+}
+
 template <int N>
 static cudaError_t launch_cfg(int op, const ElementwiseArgs *args, cudaStream_t stream, int sms) {
   if ((int)args->n > N) return cudaErrorInvalidValue;
@@ -110,6 +201,7 @@ static cudaError_t launch_cfg(int op, const ElementwiseArgs *args, cudaStream_t 
     return c < 0 ? cudaErrorInvalidValue : gfpa_launch(c, op, args, stream, sms);
   }
   switch (op) {
+    case OP_MUL: return launch_tmul<N>(*args, stream, sms);
     case OP_DIV: return launch_tnewton<OP_DIV, N>(*args, stream, sms);
     case OP_SQRT: return launch_tnewton<OP_SQRT, N>(*args, stream, sms);
   }

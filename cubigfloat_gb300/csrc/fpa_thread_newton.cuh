@@ -155,13 +155,21 @@ __device__ __forceinline__ int tround_store(const uint32_t *X, int xlen, int n, 
   const uint32_t lsb = (X[TS * q] >> s) & 1u;
   uint32_t carry = round_up(mode, sign, lsb, rbit, st) ? 1u : 0u;
   uint32_t cur = X[TS * q];
-  for (int i = 0; i < n; i++) {
+  auto limb = [&](int i) {                           // mantissa limb i, rounded
     const uint32_t nxt = (q + i + 1 < xlen) ? X[TS * (q + i + 1)] : 0u;
     uint32_t v = s ? ((cur >> s) | (nxt << (32 - s))) : cur;
     v += carry;
     carry = (carry && v == 0u) ? 1u : 0u;
-    r[i] = v;
     cur = nxt;
+    return v;
+  };
+  if ((((uintptr_t)r) & 15) == 0 && (n & 3) == 0) {  // 16-byte stores: a quarter of the transactions
+    for (int i = 0; i < n; i += 4) {
+      const uint32_t v0 = limb(i), v1 = limb(i + 1), v2 = limb(i + 2), v3 = limb(i + 3);
+      *reinterpret_cast<uint4 *>(r + i) = make_uint4(v0, v1, v2, v3);
+    }
+  } else {
+    for (int i = 0; i < n; i++) r[i] = limb(i);
   }
   ovf = (int)carry;
   if (carry) {                                       // 0.11..1 + ulp = 1.0
@@ -642,6 +650,64 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
   int ovf;
   const int Lb = tround_store(Xr, n + 2, n, sticky, mode, 0u, r, ovf);
   *r_exp = exp_word(eh - 32LL * n - 1 + Lb + ovf, 0u);
+  return 0;
+}
+
+
+// ---- mul ---------------------------------------------------------------------------------
+// One thread per multiplication.  The product of two normalised n-limb mantissas has its
+// top bit at 64n-1 or 64n-2, so the result is product limbs n-1 .. 2n-1 shifted by 0 or 1
+// bit and rounded at bit 31 or 30 of limb n-1.  The first pass forms only the output
+// blocks from c0 = 8*blk(n-1) up (a short product: about n^2/2 + 8n of the n^2 limb
+// products), without the carry from the columns below c0, which is less than c0+1 units
+// of limb c0+1.  When the bits between limb c0+1 and the round bit are neither within
+// 2^16 units of zero nor of all ones, that carry cannot reach the round bit or make the
+// bits below it zero, so the round bit is exact and sticky is 1.  Otherwise (exact ties
+// and near-ties, about 2^-170 of random operands) the operation returns 1 and is run again
+// with exact = true, which forms the whole product.  Same results as op_mul / row_mul:
+// reference fpa_warp_mul.h:41-139 (TINY when BIAS+e < 5, INF when BIAS+e > 0x7FFFFFFF).
+// A and B are zero-guarded buffers (A read as the first factor, B as the second); the
+// product limbs n-1 .. 2n-1 go to Q (n+1 limbs).
+__device__ __forceinline__ int tmul_op(uint32_t *A, uint32_t *B, uint32_t *Q, int n, int mode, uint32_t a_exp,
+                                       const uint32_t *a, uint32_t b_exp, const uint32_t *b, uint32_t *r_exp,
+                                       uint32_t *r, bool exact) {
+  const uint32_t act = c_action[2][classify(a_exp) * 9 + classify(b_exp)];
+  if (act != ACT_MUL) { *r_exp = act; return 0; }
+  stage_limbs(A, a, n);
+  stage_limbs(B, b, n);
+  const int cb0 = exact ? 0 : blk(n - 1), c0 = 8 * cb0;
+  uint32_t low = 0u;                                   // exact: OR of limbs 0 .. n-2
+  uint32_t l1 = 0u, midz = 0u, mido = 0xFFFFFFFFu;     // short: limb c0+1; OR / AND of limbs c0+2 .. n-2
+  tprod(PV{A}, n, PV{B}, n, cb0, 1 << 20, [&](int cb, const uint32_t (&o)[10]) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int p = 8 * cb + q;
+      if (p < n - 1) {
+        low |= o[q];
+        if (p == c0 + 1) l1 = o[q];
+        else if (p > c0 + 1) { midz |= o[q]; mido &= o[q]; }
+      } else if (p < 2 * n) {
+        Q[TS * (p - (n - 1))] = o[q];
+      }
+    }
+  });
+  const uint32_t full = Q[TS * n] >> 31;               // top bit at 64n-1
+  const uint32_t below = full ? 0x7FFFFFFFu : 0x3FFFFFFFu;
+  const uint32_t rl = Q[0] & below;                    // limb n-1's bits below the round bit
+  uint32_t sticky = low != 0u;
+  if (!exact && c0 > 0) {
+    const bool near0 = midz == 0u && l1 < (1u << 16) && rl == 0u;
+    const bool near1 = mido == 0xFFFFFFFFu && l1 >= 0xFFFF0000u && rl == below;
+    if (near0 || near1) return 1;
+    sticky = 1u;
+  }
+  const uint32_t sign = (a_exp ^ b_exp) & 1u;
+  int ovf;
+  const int Lb = tround_store(Q, n + 1, n, sticky, mode, sign, r, ovf);
+  const long long e = (long long)(a_exp >> 1) + (long long)(b_exp >> 1) - 2LL * BIAS - 32LL * n - 32 + Lb + ovf;
+  if ((long long)BIAS + e < 5) *r_exp = CLS_POS_TINY - sign;
+  else if ((long long)BIAS + e > 0x7FFFFFFFLL) *r_exp = CLS_POS_INF - sign;
+  else *r_exp = exp_word(e, sign);
   return 0;
 }
 

@@ -13,8 +13,8 @@ SHAPES = [(4, 2, 1), (8, 2, 1), (8, 4, 1), (16, 4, 1), (32, 4, 1), (32, 8, 1), (
 
 
 def supports(cfg, op):
-    if cfg >= 18:                      # one thread per operation: div and sqrt
-        return op in (3, 4)
+    if cfg >= 18:                      # one thread per operation: mul, div and sqrt
+        return op in (2, 3, 4)
     return cfg < 16 or op <= 1 or (cfg == 16 and op == 2)
 
 
