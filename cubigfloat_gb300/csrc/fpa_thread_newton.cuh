@@ -27,15 +27,21 @@
 // load while the current one multiplies, and no bounds checks: every buffer a product reads
 // sits in zero guard limbs, so the tiles may read past either end (an operand read as the
 // product's second factor needs 8 zero limbs below it and zeros up to 8 limbs past its
-// length rounded up to 8; the first factor only the zeros above).
+// length rounded up to 8; the first factor only the zeros above).  The loads of the next
+// tile read up to 8 more limbs below a second factor and past a first factor (not used):
+// they lie inside the layouts below.
 //
 // Storage.  A thread's limb j of a buffer is at base[32*j] (the warp's 32 threads
 // interleaved limb by limb, so the 32 threads reading one limb index touch 32 consecutive
-// words).  Workspace (shared memory): three slots of N/2+8 limbs with zero guards, holding
-// the Newton iterates and residuals, then q0 / S0 and the remainder D.  Slab (global
-// memory, one per CTA, laid out the same way): B and A (div) or Xh = floor(A 2^(32-odd))
-// (sqrt), staged once per operation from the caller's natural layout so that every later
-// operand read is one coalesced warp load, and the extra-limb result Q' / S'.
+// words).  Workspace (shared memory): two slots of N/2+8 limbs with zero guards, holding the
+// Newton iterate and the residual, then q0 / S0.  Slab (global memory, one per CTA, laid
+// out the same way): B and A (div) or Xh = floor(A 2^(32-odd)) (sqrt), staged once per
+// operation from the caller's natural layout so that every later operand read is one
+// coalesced warp load; the next iterate (copied back to shared memory at the end of each
+// level), sqrt's V1 and the remainder D, which are only read as a product's first factor;
+// and the extra-limb result Q' / S'.  Every product thus has its second factor, the one
+// whose window moves with each tile, in shared memory, and a warp's workspace (23.5 KB at
+// N = 128) leaves room for 9 warps per SM.
 //
 // Operands a, b and the result r are the caller's arrays in the natural layout (number i's
 // limbs contiguous).  Reference semantics as op_div / op_sqrt: fpa_warp_div.h:127-201,
@@ -51,13 +57,15 @@ constexpr int GUARD = 2;    // limbs formed below the lowest limb a short produc
 template <int N>
 struct TSpace {
   static constexpr int SLOT = N / 2 + 8;                       // limbs per slot (multiple of 8)
-  // workspace (shared memory), in limbs: 8 readable + 8 zero | slot | 8 zero | slot | 8 zero |
-  // slot | 8 zero + 8 readable
-  static constexpr int Z0 = 16, Z1 = Z0 + SLOT + 8, Z2 = Z1 + SLOT + 8;
+  // workspace (shared memory), in limbs: 8 readable + 8 zero | slot 0 | 8 zero | slot 2 |
+  // 8 zero + 8 readable.  Slot 0 holds the Newton iterate, slot 2 the residual, then q0 / S0.
+  static constexpr int Z0 = 16, Z2 = Z0 + SLOT + 8;
   static constexpr int words = Z2 + SLOT + 16;
-  // slab (global memory), in limbs: 16 zero | B | 16 zero | A or Xh | 16 zero | Q' or S'
-  static constexpr int SB = 16, SA = SB + N + 16, SQ = SA + N + 16;
-  static constexpr int slab = SQ + N + 8;
+  // slab (global memory), in limbs: 16 zero | B | 16 zero | A or Xh | 16 zero | Q' or S' |
+  // slot 1 (the next iterate, sqrt's V1, then the remainder D: each read only as a product's
+  // first factor) | 8 zero + 8 readable
+  static constexpr int SB = 16, SA = SB + N + 16, SQ = SA + N + 16, S1 = SQ + N + 16;
+  static constexpr int slab = S1 + SLOT + 16;
   static constexpr int min_limbs = 8;                          // smaller numbers keep the lane-group path
 };
 
@@ -196,7 +204,7 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
   int lv[24];
   const int nl = newton_levels(n, lv);
   const int l0 = small_levels_end(lv, nl, true);
-  uint32_t *Y = w + TS * S::Z0, *Y2 = w + TS * S::Z1, *E = w + TS * S::Z2;
+  uint32_t *Y = w + TS * S::Z0, *Y2 = slab + TS * S::S1, *E = w + TS * S::Z2;
   {
     const uint64_t y = 0xFFFFFFFFFFFFFFFFull / (uint64_t)SB[TS * (n - 1)];   // level 1: floor((2^64-1)/B_top)
     uint32_t v[SMALL_LEVEL + 1], bt[SMALL_LEVEL];
@@ -245,8 +253,8 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
       }
     });
     for (int i = next; i <= kp; i++) put(i, 0u);
-    zero_tail(Y2, kp + 1);
-    uint32_t *t = Y; Y = Y2; Y2 = t;
+    for (int i = 0; i <= kp; i++) Y[TS * i] = Y2[TS * i];       // back to shared memory
+    zero_tail(Y, kp + 1);
   }
   // Karp-Markstein step with one limb more than the result (op_div): h = the last Newton
   // level, m = n+2-h.  q0 = floor(A_top Y / 2^(32(h+1))), A_top = the top m+1 limbs of A.
@@ -315,7 +323,7 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
   }
   if (!exact) return 1;
   // exact correction: Qc = floor(Q'/2^32) (n+1 limbs, from limb 1 of Q'),
-  // Rm = (A 2^(32n) - Qc B) mod 2^(32(n+2)) over slots 0 and 1 (their guard limbs between
+  // Rm = (A 2^(32n) - Qc B) mod 2^(32(n+2)) over slots 0 and 2 (the guard limbs between
   // them are cleared again at the end)
   uint32_t *Qc = Q + TS, *Rm = w + TS * S::Z0;
   const uint32_t qt = Qc[TS * n];
@@ -383,7 +391,7 @@ __device__ int tdiv(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_exp
     nz |= Rm[TS * i];
     if (c2 == 0 && x != y) c2 = x > y ? 1 : -1;
   }
-  for (int i = S::SLOT; i < S::SLOT + 8; i++) Rm[TS * i] = 0u;   // the guard limbs between slots 0 and 1
+  for (int i = S::SLOT; i < S::SLOT + 8; i++) Rm[TS * i] = 0u;   // the guard limbs between slots 0 and 2
   const uint32_t rb = c2 >= 0 ? 1u : 0u, sticky = (nz != 0u && c2 != 0) ? 1u : 0u;
   // X = 2Qc + rb, n+2 limbs, formed in place one limb below Qc (limb i of X over limb i of Q')
   uint32_t *X = Q;
@@ -427,7 +435,7 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
   int lv[24];
   const int nl = newton_levels(n, lv);
   const int l0 = small_levels_end(lv, nl, true);
-  uint32_t *Z = w + TS * S::Z0, *Z2 = w + TS * S::Z1, *E = w + TS * S::Z2;
+  uint32_t *Z = w + TS * S::Z0, *Z2 = slab + TS * S::S1, *E = w + TS * S::Z2;
   {
     const uint64_t x1 = (uint64_t)X[TS * n] << 32;
     const uint64_t s1 = isqrt64(x1);
@@ -492,8 +500,8 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
       }
     });
     for (int i = next; i <= kp; i++) put(i, i == next ? (prev >> 1) : 0u);
-    zero_tail(Z2, kp + 1);
-    uint32_t *t = Z; Z = Z2; Z2 = t;
+    for (int i = 0; i <= kp; i++) Z[TS * i] = Z2[TS * i];       // back to shared memory
+    zero_tail(Z, kp + 1);
   }
   // Karp-Markstein with one limb more (op_sqrt): S0 = floor(Xt Z / 2^(32(h+1))),
   // Xt = the top m+1 limbs of Xh
@@ -566,7 +574,7 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
   }
   if (!exact) return 1;
   // exact correction: Sc = floor(S'/2^32) (n+1 limbs), Rm = (A_ext - Sc^2) mod 2^(32(n+2))
-  // over slots 0 and 1
+  // over slots 0 and 2
   uint32_t *Sc = Sq + TS, *Rm = w + TS * S::Z0;
   const VW xh{X, n + 1};
   const uint32_t stop = Sc[TS * n];
@@ -640,7 +648,7 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
     nz |= x;
     if (c2 == 0 && x != y) c2 = x > y ? 1 : -1;
   }
-  for (int i = S::SLOT; i < S::SLOT + 8; i++) Rm[TS * i] = 0u;   // the guard limbs between slots 0 and 1
+  for (int i = S::SLOT; i < S::SLOT + 8; i++) Rm[TS * i] = 0u;   // the guard limbs between slots 0 and 2
   const uint32_t rb = c2 > 0 ? 1u : 0u, sticky = nz != 0u ? 1u : 0u;
   uint32_t *Xr = Sq;                                  // 2Sc + rb in place one limb below Sc
   for (int i = 0; i < n + 2; i++) {
