@@ -218,6 +218,68 @@ def mpfr_leg(data, gpu_results, threads, count=MPFR_SAMPLE):
             "gpu_sample_bit_exact_vs_mpfr": exact if gpu_results is not None else None}
 
 
+# The one-thread kernels (configuration 18: k_tmul, k_tnewton in fpa_thread_newton.cu) form
+# fewer limb products than the schoolbook basis counts: mul a short product above the
+# rounding limb, div and sqrt Newton levels and a Karp-Markstein step whose products are
+# restricted to the limbs that are read.  tile_products() mirrors their 8x8-tile block
+# ranges (tprod: output blocks [cb_lo, cb_hi) of an lx x ly product, block cb spanning
+# x blocks max(0, cb-My) .. min(cb, Mx-1)), so that the roofline can also report how busy
+# the multiplier is on the products the first pass executes (deferred operations excluded).
+KERNELS = {"mul": "k_tmul<128>", "div": "k_tnewton<3 (div), 128>", "sqrt": "k_tnewton<4 (sqrt), 128>"}
+
+
+def _tprod_tiles(lx, ly, cb_lo, cb_hi):
+    mx, my = (lx + 7) // 8, (ly + 7) // 8
+    return sum(min(cb, mx - 1) - max(0, cb - my) + 1 for cb in range(cb_lo, min(mx + my, cb_hi)))
+
+
+def _levels(n):
+    out, k = [n], n
+    while k > 1:
+        p = (k + 2) // 2
+        k = k - 1 if p >= k else p
+        out.append(k)
+    return out[::-1]
+
+
+def tile_products(op, n):
+    """Limb products (64 per 8x8 tile) of the first pass of one operation at n limbs."""
+    blk = lambda keep: max(0, keep - 2) // 8
+    big = 1 << 20
+    if op == "mul":
+        return 64 * _tprod_tiles(n, n, blk(n - 1), big)
+    lv = _levels(n)
+    e = 1
+    while e < len(lv) - 1 and lv[e] <= 9:          # one-thread register levels
+        e += 1
+    tiles = 0
+    for li in range(e, len(lv) - 1):
+        k, kp = lv[li - 1], lv[li]
+        lt = kp - k + 3
+        if op == "div":
+            tiles += _tprod_tiles(kp, k + 1, blk(k - 1), (k + kp) // 8 + 1)
+            tiles += _tprod_tiles(k + 1, lt, blk(k + 1), (k + 1 + lt + 7) // 8)
+        else:
+            j = k - 2 if k > 2 else 0
+            l1, L, off = kp + k + 1 - j, kp + 2 * k - j, 2 * k - 1 - j
+            tiles += _tprod_tiles(kp, k + 1, blk(j), (j + l1 + 7) // 8)
+            tiles += _tprod_tiles(l1, k + 1, blk(off), L // 8 + 1)
+            tiles += _tprod_tiles(k + 1, lt, blk(k + 1), big)
+    h = lv[-2]
+    m = n + 2 - h
+    if op == "div":
+        dlen, sh = m + 2, n - h - 1
+        tiles += _tprod_tiles(m + 1, h + 1, blk(h + 1), (h + m + 9) // 8)
+        tiles += _tprod_tiles(m + 1, n, blk(sh), (sh + dlen + 7) // 8)
+        tiles += _tprod_tiles(dlen, h + 1, blk(h + 2), (dlen + h + 8) // 8)
+    else:
+        dlen, ssh = m + 3, 2 * h - n
+        tiles += _tprod_tiles(m + 1, h + 1, blk(h + 1), (h + m + 9) // 8)
+        tiles += _tprod_tiles(m + 1, m + 1, 0, (dlen - ssh + 7) // 8)
+        tiles += _tprod_tiles(dlen, h + 1, blk(h + 3), big)
+    return 64 * tiles
+
+
 def load_traffic():
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if os.path.exists(path):
@@ -737,7 +799,8 @@ def run_gb300(args):
     dom = max(OPS, key=lambda o: per_op_ms[o])
     achieved = PRODUCTS[dom] * count / (per_op_ms[dom] / 1e3) / 1e12
     traffic = load_traffic().get(f"{dom}_n{n}")
-    roofline = {"bound": "int-multiply", "kernel": f"k_elementwise<{dom}>, 4096-bit",
+    roofline = {"bound": "int-multiply", "kernel": f"{KERNELS[dom]}, 4096-bit (first pass and the deferred "
+                                                  "operations' exact pass, one fpa call)",
                 "achieved": round(achieved, 4), "peak": round(prod_peak / 1e12, 4), "unit": "T limb products/s",
                 "frac": round(achieved / (prod_peak / 1e12), 4),
                 "peak_source": "measured live on this GPU: mad.lo.cc + madc.hi.cc + addc per 32x32-bit limb "
@@ -747,7 +810,10 @@ def run_gb300(args):
                 "isolated_instruction_peaks": {"mad_lo_T_per_s": round(lo / 1e12, 3), "mad_hi_T_per_s": round(hi / 1e12, 3)},
                 "traffic": traffic,
                 "per_op": {op: {"ms": round(per_op_ms[op], 3), "ops_s": round(count / (per_op_ms[op] / 1e3), 1),
-                                "product_frac": round(PRODUCTS[op] * count / (per_op_ms[op] / 1e3) / prod_peak, 4)}
+                                "product_frac": round(PRODUCTS[op] * count / (per_op_ms[op] / 1e3) / prod_peak, 4),
+                                "executed_products_per_op": tile_products(op, n),
+                                "executed_frac": round(tile_products(op, n) * count / (per_op_ms[op] / 1e3) / prod_peak,
+                                                       4)}
                            for op in OPS}}
     cpu, bit_exact = None, None
     if not args.no_cpu:

@@ -104,12 +104,22 @@ __device__ __forceinline__ void zero_tail(uint32_t *p, int len) {
 // Output block cb gathers x-block i times the y window y[8(cb-i)-8 .. 8(cb-i)+7] for every i
 // with 0 <= cb-i <= My (My = y's block count), into 96-bit (lo, hi, top) column sums fed by
 // mac3; the two limbs above a block carry into the next one (none into block cb_lo).
-// sink(cb, L) receives limbs 8cb .. 8cb+7 in L[0..7].
-template <class X, class Y, class Sink>
+// sink(cb, L) receives limbs 8cb .. 8cb+7 in L[0..7].  NEXT: the next block's first-tile
+// operands load while the current block computes (24 more live registers: a gain for mul's
+// kernel, a loss where registers are already scarce, as in div and sqrt).
+template <bool NEXT = false, class X, class Y, class Sink>
 __device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, int cb_lo, int cb_hi, Sink &&sink) {
   const int Mx = (lx + 7) >> 3, My = (ly + 7) >> 3;
   const int Mo = min(Mx + My, cb_hi);
   uint32_t c0 = 0u, c1 = 0u;
+  uint32_t a0[8], w0[16];
+  if (NEXT) {
+    const int i0 = max(0, cb_lo - My);
+#pragma unroll
+    for (int r = 0; r < 8; r++) a0[r] = x.get(8 * i0 + r);
+#pragma unroll
+    for (int m = 0; m < 16; m++) w0[m] = y.get(8 * (cb_lo - i0) - 8 + m);
+  }
 #pragma unroll 1
   for (int cb = cb_lo; cb < Mo; cb++) {
     uint32_t lo[8], hi[8], tp[8];
@@ -118,10 +128,22 @@ __device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, in
     lo[0] = c0; lo[1] = c1;
     const int i0 = max(0, cb - My), i1 = min(cb, Mx - 1);
     uint32_t a[8], w[16];
+    if (NEXT) {
 #pragma unroll
-    for (int r = 0; r < 8; r++) a[r] = x.get(8 * i0 + r);
+      for (int r = 0; r < 8; r++) a[r] = a0[r];
 #pragma unroll
-    for (int m = 0; m < 16; m++) w[m] = y.get(8 * (cb - i0) - 8 + m);
+      for (int m = 0; m < 16; m++) w[m] = w0[m];
+      const int j0 = max(0, cb + 1 - My);   // block cb+1's first tile (read past the end on the last block)
+#pragma unroll
+      for (int r = 0; r < 8; r++) a0[r] = x.get(8 * j0 + r);
+#pragma unroll
+      for (int m = 0; m < 16; m++) w0[m] = y.get(8 * (cb + 1 - j0) - 8 + m);
+    } else {
+#pragma unroll
+      for (int r = 0; r < 8; r++) a[r] = x.get(8 * i0 + r);
+#pragma unroll
+      for (int m = 0; m < 16; m++) w[m] = y.get(8 * (cb - i0) - 8 + m);
+    }
 #pragma unroll 2
     for (int i = i0; i <= i1; i++) {
       uint32_t an[8], wn[8];              // the next tile's operands, loaded ahead of the math
@@ -686,7 +708,7 @@ __device__ __forceinline__ int tmul_op(uint32_t *A, uint32_t *B, uint32_t *Q, in
   const int cb0 = exact ? 0 : blk(n - 1), c0 = 8 * cb0;
   uint32_t low = 0u;                                   // exact: OR of limbs 0 .. n-2
   uint32_t l1 = 0u, midz = 0u, mido = 0xFFFFFFFFu;     // short: limb c0+1; OR / AND of limbs c0+2 .. n-2
-  tprod(PV{A}, n, PV{B}, n, cb0, 1 << 20, [&](int cb, const uint32_t (&o)[10]) {
+  tprod<true>(PV{A}, n, PV{B}, n, cb0, 1 << 20, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int p = 8 * cb + q;

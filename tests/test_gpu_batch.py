@@ -113,9 +113,9 @@ def test_batch_rejects_bad_descriptors():
 
 
 def config_runs(cfg, op):
-    """16: add/sub/mul, 17: add/sub, 18 and 19: div/sqrt, the others every operation"""
+    """16: add/sub/mul, 17: add/sub, 18 and 19: mul/div/sqrt, the others every operation"""
     if cfg >= 18:
-        return op in (3, 4)
+        return op in (2, 3, 4)
     return cfg < 16 or op <= (2 if cfg == 16 else 1)
 
 
