@@ -52,6 +52,7 @@ def _units():
         units.append(("fpa_batch_kernels.cu", [f"-DGFPA_BATCH_CLASS={c}"], f"fpa_batch_kernels_cls{c}.o"))
     units.append(("fpa_serve.cu", [], "fpa_serve.o"))
     units.append(("fpa_thread_newton.cu", [], "fpa_thread_newton.o"))
+    units.append(("fpa_batch_thread.cu", [], "fpa_batch_thread.o"))
     return [u for u in units if os.path.exists(os.path.join(CSRC, u[0]))]
 
 

@@ -9,6 +9,10 @@
 // Run: one persistent kernel per non-empty class (fpa_batch_kernels.cu), class 0 on the
 // caller's stream and classes 1 and 2 on forked side streams so they share the GPU
 // concurrently; a run can be captured once as a CUDA graph and replayed with one launch.
+// Batches created by fpa_batch_create also send mul, div and sqrt of 8 to 128 limbs whose
+// tuned configuration is a one-thread one to a fourth class (fpa_batch_thread.cu: tasks of
+// up to 32 operations of one operation and limb count, one operation per thread, its two
+// launches on the caller's stream after class 0).
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <vector>
@@ -90,7 +94,7 @@ cudaError_t gfpa_batch_launch_class(int c, const BatchArgs *a, int grid, size_t 
   return launch(c, a, grid, smem, st);
 }
 
-fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan) {
+fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan, bool one_thread) {
   if (count > 0xFFFFFFFFull) return fpa_invalid_counts;
   if (count && !descs) return fpa_math_error;
   std::vector<uint32_t> &order = plan.order;
@@ -101,21 +105,28 @@ fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms,
     const fpa_batch_desc &d = descs[i];
     if (d.op > 4 || d.mode > 4) return fpa_math_error;
     if (d.limbs == 0 || d.limbs > GFPA_MAX_LIMBS) return fpa_invalid_precisions;
+    order[i] = (uint32_t)i;
+    const int tcfg = one_thread && d.op >= OP_MUL && d.limbs >= 8 && d.limbs <= 128 ? gfpa_cfg_for_op(d.op, d.limbs) : -1;
+    if (tcfg == 18 || tcfg == 19) {                       // one thread per operation
+      key[i] = (uint16_t)(18 * 5 + d.op);
+      cls[i] = (uint8_t)GFPA_THREAD_CLASS;
+      continue;
+    }
     const int cfg = gfpa_batch_cfg_for(d.op, d.limbs);
     if (cfg < 0) return fpa_invalid_precisions;
     key[i] = (uint16_t)(cfg * 5 + d.op);
     cls[i] = (uint8_t)gfpa_class_of(cfg, d.op);
-    order[i] = (uint32_t)i;
   }
   std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
     if (cls[x] != cls[y]) return cls[x] < cls[y];
     if (key[x] != key[y]) return key[x] < key[y];
     return descs[x].limbs > descs[y].limbs;
   });
-  std::vector<BatchTask> tasks[3];
-  std::vector<double> cost[3];
+  std::vector<BatchTask> tasks[4];
+  std::vector<double> cost[4];
   uint64_t i = 0;
-  while (i < count) {
+  plan.thread_ops = 0;
+  while (i < count && cls[order[i]] != GFPA_THREAD_CLASS) {
     uint64_t j = i;
     const uint16_t k = key[order[i]];
     while (j < count && key[order[j]] == k) j++;
@@ -133,21 +144,44 @@ fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms,
     }
     i = j;
   }
+  // one-thread class: runs of one (operation, limb count), 32 operations per task
+  while (i < count) {
+    uint64_t j = i;
+    const fpa_batch_desc &d0 = descs[order[i]];
+    while (j < count && descs[order[j]].op == d0.op && descs[order[j]].limbs == d0.limbs) j++;
+    for (uint64_t s = i; s < j; s += 32) {
+      BatchTask t;
+      t.key = (uint16_t)(18 * 5 + d0.op); t.pad = 0; t.first = (uint32_t)s;
+      t.count = (uint32_t)std::min<uint64_t>(32, j - s);
+      tasks[GFPA_THREAD_CLASS].push_back(t);
+      cost[GFPA_THREAD_CLASS].push_back(op_weight(d0.op, d0.limbs));
+    }
+    plan.thread_ops += j - i;
+    i = j;
+  }
   plan.tasks.clear();
-  for (int c = 0; c < 3; c++) {
+  for (int c = 0; c < 4; c++) {
     std::vector<size_t> idx(tasks[c].size());
     for (size_t q = 0; q < idx.size(); q++) idx[q] = q;
     std::stable_sort(idx.begin(), idx.end(), [&](size_t x, size_t y) { return cost[c][x] > cost[c][y]; });
     plan.task_base[c] = (uint32_t)plan.tasks.size();
     plan.ntasks[c] = (uint32_t)idx.size();
-    uint32_t ww = 0;
-    for (size_t q : idx) {
-      plan.tasks.push_back(tasks[c][q]);
-      ww = std::max<uint32_t>(ww, (uint32_t)warp_words_for(tasks[c][q].key / 5, tasks[c][q].key % 5));
+    for (size_t q : idx) plan.tasks.push_back(tasks[c][q]);
+    plan.grid[c] = 0;
+    if (c == GFPA_THREAD_CLASS) {
+      plan.smem[c] = gfpa_batch_thread_smem();
+      if (plan.ntasks[c]) {
+        int per = 0;
+        if (gfpa_batch_thread_prepare(&per) != cudaSuccess) return fpa_device_error;
+        if (per < 1) per = 1;
+        plan.grid[c] = (int)std::min<uint64_t>((uint64_t)per * sms, plan.ntasks[c]);
+      }
+      continue;
     }
+    uint32_t ww = 0;
+    for (size_t q : idx) ww = std::max<uint32_t>(ww, (uint32_t)warp_words_for(tasks[c][q].key / 5, tasks[c][q].key % 5));
     plan.warp_words[c] = ww;
     plan.smem[c] = (size_t)(gfpa_class_threads[c] / 32) * ww * 4;
-    plan.grid[c] = 0;
     if (plan.smem[c] > 227 * 1024) return fpa_device_error;
     if (plan.ntasks[c]) {
       int per = 0;
@@ -163,7 +197,7 @@ cudaError_t gfpa_batch_enqueue(const BatchPlan &plan, const fpa_batch_desc *d_de
                                const BatchTask *d_tasks, uint32_t *d_counters, uint32_t *r_exps, uint32_t *r_limbs,
                                const uint32_t *a_exps, const uint32_t *a_limbs, const uint32_t *b_exps,
                                const uint32_t *b_limbs, cudaStream_t st, const cudaStream_t side[2],
-                               cudaEvent_t fork, const cudaEvent_t join[2]) {
+                               cudaEvent_t fork, const cudaEvent_t join[2], const ThreadScratch *ts) {
   uint32_t *err;
   int sms;
   if (!gfpa_context(&sms, &err)) return cudaErrorUnknown;
@@ -185,6 +219,17 @@ cudaError_t gfpa_batch_enqueue(const BatchPlan &plan, const fpa_batch_desc *d_de
     A.warp_words = plan.warp_words[c];
     if ((e = launch(c, &A, plan.grid[c], plan.smem[c], streams[c])) != cudaSuccess) return e;
   }
+  if (plan.ntasks[GFPA_THREAD_CLASS]) {
+    if (!ts || !ts->slabs) return cudaErrorInvalidValue;
+    ThreadBatchArgs T;
+    T.b = A;
+    T.b.tasks = d_tasks + plan.task_base[GFPA_THREAD_CLASS];
+    T.b.ntasks = plan.ntasks[GFPA_THREAD_CLASS];
+    T.b.counter = d_counters + GFPA_THREAD_CLASS;
+    T.b.warp_words = 0;
+    T.slabs = ts->slabs; T.hard_count = ts->hard_count; T.hard_idx = ts->hard_idx;
+    if ((e = gfpa_batch_thread_launch(&T, plan.grid[GFPA_THREAD_CLASS], st)) != cudaSuccess) return e;
+  }
   for (int c = 1; c < 3; c++) {
     if ((e = cudaEventRecord(join[c - 1], streams[c])) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(st, join[c - 1], 0)) != cudaSuccess) return e;
@@ -199,6 +244,7 @@ struct fpa_batch_s {
   uint32_t *d_order = nullptr;
   BatchTask *d_tasks = nullptr;
   uint32_t *d_counters = nullptr;     // one per class
+  ThreadScratch ts;                   // the one-thread class's slabs and deferred list
   cudaStream_t side[2] = {nullptr, nullptr};
   cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
   cudaGraph_t graph = nullptr;
@@ -212,7 +258,7 @@ extern "C" fpa_result fpa_batch_create(fpa_batch_t *out, const fpa_batch_desc *d
   if (!gfpa_context(&sms, nullptr)) return fpa_device_error;
   fpa_batch_s *b = new fpa_batch_s();
   b->count = count;
-  fpa_result r = gfpa_batch_plan(descs, count, sms, b->plan);
+  fpa_result r = gfpa_batch_plan(descs, count, sms, b->plan, true);
   if (r != fpa_success) { delete b; return r; }
   const std::vector<BatchTask> &all = b->plan.tasks;
   bool ok = true;
@@ -220,6 +266,11 @@ extern "C" fpa_result fpa_batch_create(fpa_batch_t *out, const fpa_batch_desc *d
   ok = ok && cudaMalloc(&b->d_order, std::max<size_t>(1, count) * 4) == cudaSuccess;
   ok = ok && cudaMalloc(&b->d_tasks, std::max<size_t>(1, all.size()) * sizeof(BatchTask)) == cudaSuccess;
   ok = ok && cudaMalloc(&b->d_counters, 16) == cudaSuccess;
+  if (ok && b->plan.ntasks[GFPA_THREAD_CLASS]) {
+    ok = cudaMalloc(&b->ts.slabs, gfpa_batch_thread_slab_bytes(b->plan.grid[GFPA_THREAD_CLASS])) == cudaSuccess &&
+         cudaMalloc(&b->ts.hard_count, 256) == cudaSuccess &&
+         cudaMalloc(&b->ts.hard_idx, std::max<size_t>(1, b->plan.thread_ops) * 4) == cudaSuccess;
+  }
   if (ok && count)
     ok = cudaMemcpy(b->d_descs, descs, count * sizeof(fpa_batch_desc), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(b->d_order, b->plan.order.data(), count * 4, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -239,7 +290,7 @@ static cudaError_t batch_enqueue(fpa_batch_t b, uint32_t *r_exps, uint32_t *r_li
                                  const uint32_t *a_limbs, const uint32_t *b_exps, const uint32_t *b_limbs,
                                  cudaStream_t st) {
   return gfpa_batch_enqueue(b->plan, b->d_descs, b->d_order, b->d_tasks, b->d_counters, r_exps, r_limbs, a_exps,
-                            a_limbs, b_exps, b_limbs, st, b->side, b->ev_fork, b->ev_join);
+                            a_limbs, b_exps, b_limbs, st, b->side, b->ev_fork, b->ev_join, &b->ts);
 }
 
 extern "C" fpa_result fpa_batch_run(fpa_batch_t b, uint32_t *r_exps, uint32_t *r_limbs, const uint32_t *a_exps,
@@ -289,6 +340,7 @@ extern "C" fpa_result fpa_batch_info(fpa_batch_t b, uint32_t *tasks_per_class, u
     if (tasks_per_class) tasks_per_class[c] = b->plan.ntasks[c];
     k += b->plan.ntasks[c] ? 1 : 0;
   }
+  k += b->plan.ntasks[GFPA_THREAD_CLASS] ? 1 : 0;
   if (kernels) *kernels = k;
   return fpa_success;
 }
@@ -303,6 +355,7 @@ extern "C" fpa_result fpa_batch_destroy(fpa_batch_t b) {
     if (b->side[c]) cudaStreamDestroy(b->side[c]);
   }
   cudaFree(b->d_descs); cudaFree(b->d_order); cudaFree(b->d_tasks); cudaFree(b->d_counters);
+  cudaFree(b->ts.slabs); cudaFree(b->ts.hard_count); cudaFree(b->ts.hard_idx);
   delete b;
   return fpa_success;
 }

@@ -45,26 +45,50 @@ __host__ __device__ constexpr int gfpa_class_of(int cfg, int op) {
 // threads per CTA of each class kernel
 static const int gfpa_class_threads[3] = {256, 128, 128};
 
+// The one-thread class (fpa_batch_thread.cu): the batch fields above (tasks of up to 32
+// operations of one operation and limb count, `counter` its task counter) plus this batch's
+// per-CTA slabs and the list of operations its first pass defers to the exact pass.
+struct ThreadBatchArgs {
+  BatchArgs b;
+  uint32_t *slabs;
+  uint32_t *hard_count, *hard_idx;
+};
+// Device scratch of the one-thread class, owned by the batch.
+struct ThreadScratch {
+  uint32_t *slabs = nullptr, *hard_count = nullptr, *hard_idx = nullptr;
+};
+size_t gfpa_batch_thread_smem();
+size_t gfpa_batch_thread_slab_bytes(int grid);
+cudaError_t gfpa_batch_thread_prepare(int *blocks_per_sm);
+cudaError_t gfpa_batch_thread_launch(const ThreadBatchArgs *a, int grid, cudaStream_t st);
+// the class index of the one-thread class
+constexpr int GFPA_THREAD_CLASS = 3;
+
 // Host-side plan of a batch: descriptor order, tasks (concatenated class by class) and the
-// launch shape of each class kernel.
+// launch shape of each class kernel (classes 0-2: lane groups; 3: one thread per operation).
 #include <vector>
 struct BatchPlan {
   std::vector<uint32_t> order;
   std::vector<BatchTask> tasks;
-  uint32_t ntasks[3] = {0, 0, 0}, task_base[3] = {0, 0, 0}, warp_words[3] = {0, 0, 0};
-  size_t smem[3] = {0, 0, 0};
-  int grid[3] = {0, 0, 0};
+  uint32_t ntasks[4] = {0, 0, 0, 0}, task_base[4] = {0, 0, 0, 0}, warp_words[4] = {0, 0, 0, 0};
+  size_t smem[4] = {0, 0, 0, 0};
+  int grid[4] = {0, 0, 0, 0};
+  uint64_t thread_ops = 0;    // operations of the one-thread class
 };
-// Plan `count` descriptors; fpa_success or the validation error.
-fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan);
+// Plan `count` descriptors; fpa_success or the validation error.  With `one_thread`, mul,
+// div and sqrt of 8 to 128 limbs whose tuned configuration is a one-thread one (18, 19) go to
+// the one-thread class, which needs a ThreadScratch at enqueue.
+fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan,
+                           bool one_thread = false);
 // Enqueue one run of a plan whose descriptors, order and tasks are already in device memory.
-// Class 0 runs on `st`, classes 1 and 2 on `side[0]`, `side[1]` (forked from and joined back
-// into `st` with the given events).
+// Classes 0 and 3 run on `st`, classes 1 and 2 on `side[0]`, `side[1]` (forked from and
+// joined back into `st` with the given events).  `ts`: the one-thread class's scratch (only
+// read when the plan has that class).
 cudaError_t gfpa_batch_enqueue(const BatchPlan &plan, const fpa_batch_desc *d_descs, const uint32_t *d_order,
                                const BatchTask *d_tasks, uint32_t *d_counters, uint32_t *r_exps, uint32_t *r_limbs,
                                const uint32_t *a_exps, const uint32_t *a_limbs, const uint32_t *b_exps,
                                const uint32_t *b_limbs, cudaStream_t st, const cudaStream_t side[2],
-                               cudaEvent_t fork, const cudaEvent_t join[2]);
+                               cudaEvent_t fork, const cudaEvent_t join[2], const ThreadScratch *ts = nullptr);
 
 // Planner helpers shared with other entry points of the batched form.
 int gfpa_batch_warp_words(int cfg, int op);          // shared-memory words per warp

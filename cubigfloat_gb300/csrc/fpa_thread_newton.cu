@@ -106,18 +106,6 @@ static cudaError_t launch_tnewton(const ElementwiseArgs &args, cudaStream_t stre
   return e != cudaSuccess ? e : ef;
 }
 
-// mul (tmul_op): A in this thread's shared-memory columns (read as the product's first
-// factor: 8 limbs per tile), B and the product limbs that feed the rounding in its slab
-// column.  Measured on GB300 at 4096 bits: A and B both in shared memory allow 5 warps per
-// SM (3.88 ms per 2^20 operations), both in the slab leave the operand reads to L2
-// (3.10 ms); this split holds 11 warps per SM (2.37 ms).  Limb offsets per thread:
-template <int N>
-struct MSpace {
-  static constexpr int words = N + 16;                  // shared memory: A, then zeros
-  static constexpr int SB = 16, GQ = N + 32;            // slab: 16 zero | B | 16 zero | Q
-  static constexpr int slab = GQ + N + 8;
-};
-
 template <int N>
 __global__ void __launch_bounds__(32) k_tmul(ElementwiseArgs args, uint32_t *ctl, uint32_t *hard_idx, uint32_t *slabs,
                                              int pass) {

@@ -69,8 +69,11 @@ struct TSpace {
   static constexpr int min_limbs = 8;                          // smaller numbers keep the lane-group path
 };
 
-// Copies n limbs of a natural-layout number to a slab column (limb j at dst[TS*j]).
+// Copies n limbs of a natural-layout number to a slab column (limb j at dst[TS*j]) and
+// clears the 16 limbs above them, the zero guard that a buffer staged for a larger limb
+// count may have left nonzero (a CTA of the batched form runs tasks of several sizes).
 __device__ __forceinline__ void stage_limbs(uint32_t *dst, const uint32_t *src, int n) {
+  for (int j = n; j < n + 16; j++) dst[TS * j] = 0u;
   if ((((uintptr_t)src) & 15) == 0 && (n & 3) == 0) {
     for (int j = 0; j < n; j += 4) {
       const uint4 v = *reinterpret_cast<const uint4 *>(src + j);
@@ -453,6 +456,7 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
       prev = cur;
     }
     X[TS * n] = odd ? (prev >> 1) : prev;
+    for (int j = n + 1; j < n + 16; j++) X[TS * j] = 0u;     // the zero guard above Xh
   }
   int lv[24];
   const int nl = newton_levels(n, lv);
@@ -683,6 +687,18 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
   return 0;
 }
 
+
+// mul (tmul_op): A in this thread's shared-memory columns (read as the product's first
+// factor: 8 limbs per tile), B and the product limbs that feed the rounding in its slab
+// column.  Measured on GB300 at 4096 bits: A and B both in shared memory allow 5 warps per
+// SM (3.88 ms per 2^20 operations), both in the slab leave the operand reads to L2
+// (3.10 ms); this split holds 11 warps per SM (2.37 ms).  Limb offsets per thread:
+template <int N>
+struct MSpace {
+  static constexpr int words = N + 16;                  // shared memory: A, then zeros
+  static constexpr int SB = 16, GQ = N + 32;            // slab: 16 zero | B | 16 zero | Q
+  static constexpr int slab = GQ + N + 8;
+};
 
 // ---- mul ---------------------------------------------------------------------------------
 // One thread per multiplication.  The product of two normalised n-limb mantissas has its

@@ -62,7 +62,9 @@ int fpa_gb300_get_config(uint32_t limbs);
  * word i of the r/a/b exponent arrays belongs to descriptor i.  The plan sorts the
  * operations into per-configuration tasks, picks each one's lane-group configuration from
  * the autotuned table, and runs them with persistent kernels (one per register class,
- * concurrent) that pull tasks from device work queues. */
+ * concurrent) that pull tasks from device work queues.  mul, div and sqrt of 8 to 128 limbs
+ * whose tuned configuration runs one thread per operation form one more class (tasks of up
+ * to 32 operations of one operation and limb count), whose device scratch the batch owns. */
 typedef struct {
   uint8_t op;          /* fpa_op */
   uint8_t mode;        /* fpa_rounding_mode */
@@ -85,7 +87,8 @@ fpa_result fpa_batch_capture(fpa_batch_t batch, uint32_t *r_exps, uint32_t *r_li
                              const uint32_t *a_exps, const uint32_t *a_limbs,
                              const uint32_t *b_exps, const uint32_t *b_limbs);
 fpa_result fpa_batch_graph_launch(fpa_batch_t batch, void *stream);
-/* number of tasks per register class (3 classes) and kernels per run, for inspection */
+/* number of tasks per lane-group register class (3 entries) and class kernels per run
+ * (the one-thread class counts as one), for inspection */
 fpa_result fpa_batch_info(fpa_batch_t batch, uint32_t *tasks_per_class, uint32_t *kernels);
 fpa_result fpa_batch_destroy(fpa_batch_t batch);
 

@@ -72,7 +72,8 @@ def test_mixed_batch_matches_oracle():
     descs["mode"] = rng.integers(0, 5, size=len(descs))
     got, info = run_batch(descs, ae, al, be, bl, total)
     tasks, kernels = info
-    assert kernels == 3 and all(t > 0 for t in tasks)
+    # the three lane-group classes and the one-thread class (mul/div/sqrt of 8-128 limbs)
+    assert kernels == 4 and all(t > 0 for t in tasks)
     check_mixed(descs, ae, al, be, bl, total, got)
 
 
