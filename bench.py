@@ -598,10 +598,84 @@ def extra_served(fpa, njobs=400, rates=(1000.0, 4000.0, 16000.0, None)):
             rec["batched" if batching else "plain"] = {
                 "ops_s": total_ops / span, "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "batches": int(st["batches"]),
-                "peak_bytes": int(st["peak_bytes"])}
+                "peak_bytes": int(st["peak_bytes"]),
+                "submit_span_ms": round((max(t[0] for t in tt) - min(t[0] for t in tt)) / 1e6, 3)}
+            if batching:
+                c = srv.costs()
+                rec["batched"]["cost_ms"] = {k[:-3]: round(v / 1e6, 3) for k, v in c.items()}
+                rec["batched"]["span_ms"] = round(span * 1e3, 3)
             srv.destroy()
+        rec["offered_ops_s"] = total_ops / max(float(arr[-1]), 1e-9) if rate else None
         rec["throughput_vs_plain"] = rec["batched"]["ops_s"] / rec["plain"]["ops_s"]
         out["burst" if rate is None else f"poisson_{int(rate)}_jobs_s"] = rec
+    out["batch_graph_same_ops"] = _served_as_one_batch(fpa, jobs, total_ops)
+    out["burst_vs_batch_graph"] = out["burst"]["batched"]["ops_s"] / out["batch_graph_same_ops"]["ops_s"]
+    out["resident_chain"] = _resident_chain(fpa)
+    return out
+
+
+def _served_as_one_batch(fpa, jobs, total_ops):
+    """The served stream's operations as one fpa_batch, operands already on the device, timed
+    as a graph launch: the device-side bound the served stream is compared with."""
+    import torch
+    rows, off = [], 0
+    for precision, ops, modes, ae, al, be, bl in jobs:
+        n = precision // 32
+        for i in range(len(ops)):
+            rows.append((ops[i], modes[i], n, off + i * n))
+        off += len(ops) * n
+    descs = np.zeros(len(rows), dtype=fpa.BATCH_DESC)
+    descs["op"] = [r[0] for r in rows]
+    descs["mode"] = [r[1] for r in rows]
+    descs["limbs"] = [r[2] for r in rows]
+    descs["a_off"] = descs["b_off"] = descs["r_off"] = [r[3] for r in rows]
+    cat = lambda k: np.concatenate([j[k] for j in jobs])
+    d_ae, d_al, d_be, d_bl = (_dev(torch, cat(k)) for k in (3, 4, 5, 6))
+    d_re = torch.zeros(len(rows), dtype=torch.int32, device="cuda")
+    d_rl = torch.zeros(off, dtype=torch.int32, device="cuda")
+    b = fpa.Batch(descs)
+    assert b.capture(d_re.data_ptr(), d_rl.data_ptr(), d_ae.data_ptr(), d_al.data_ptr(), d_be.data_ptr(),
+                     d_bl.data_ptr()) == 0
+    ms = _timed(torch, lambda: b.graph_launch())
+    b.destroy()
+    return {"ops_s": total_ops / (ms / 1e3), "ms": round(ms, 3)}
+
+
+def _resident_chain(fpa, steps=8, count=4096, precision=4096):
+    """A chain y <- RN(y * x) repeated `steps` times on one job of `count` operations: each
+    step a served job reading the previous step's kept result on the device (submitted all at
+    once), against the same chain with a host round trip per step (wait, then resubmit with
+    the result).  Both end with the same values."""
+    from cubigfloat_gb300 import workloads as W
+    rng = np.random.default_rng(8)
+    n = precision // 32
+    xe, xl = W.uniform(rng, count, n, -2, 2)
+    ye, yl = W.uniform(rng, count, n, -2, 2)
+    ops = np.full(count, 2, np.uint8)
+    out = {"workload": f"{steps} chained mul jobs of {count} ops at {precision} bits"}
+    srv = fpa.Server(hbm_budget_bytes=1 << 30, max_inflight=2, resident_bytes=256 << 20)
+    try:
+        t0 = time.perf_counter()
+        prev, _ = srv.submit(precision, ops, None, ye, yl.ravel(), xe, xl.ravel(), keep=True, copy_out=False)
+        ids = [prev]
+        for k in range(1, steps):
+            last = k == steps - 1
+            prev, res = srv.submit(precision, ops, None, None, None, xe, xl.ravel(), a_from=prev, keep=not last,
+                                   copy_out=last)
+            ids.append(prev)
+        assert srv.wait(prev, 60000) == 0
+        dev_ms = (time.perf_counter() - t0) * 1e3
+        dev_res = res
+        t0 = time.perf_counter()
+        ce, cl = ye, yl.ravel()
+        for k in range(steps):
+            jid, (ce, cl) = srv.submit(precision, ops, None, ce, cl, xe, xl.ravel())
+            assert srv.wait(jid, 60000) == 0
+        host_ms = (time.perf_counter() - t0) * 1e3
+        out.update({"device_resident_ms": round(dev_ms, 3), "host_round_trip_ms": round(host_ms, 3),
+                    "same_result": bool(np.array_equal(dev_res[0], ce) and np.array_equal(dev_res[1], cl))})
+    finally:
+        srv.destroy()
     return out
 
 

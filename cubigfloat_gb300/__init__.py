@@ -36,6 +36,12 @@ class FpaError(RuntimeError):
     pass
 
 
+class ServerJobOpts(ctypes.Structure):
+    """fpa_gb300.h: fpa_server_job_opts"""
+    _fields_ = [("a_from", ctypes.c_int64), ("b_from", ctypes.c_int64), ("keep", ctypes.c_uint32),
+                ("copy_out", ctypes.c_uint32)]
+
+
 class ServerConfig(ctypes.Structure):
     """fpa_gb300.h: fpa_server_config"""
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
@@ -103,6 +109,11 @@ def lib():
                                        ctypes.POINTER(u64)]),
         "fpa_server_release": (i32, [vp, ctypes.c_int64]),
         "fpa_server_stats": (i32, [vp, ctypes.POINTER(u64)]),
+        "fpa_server_create_resident": (i32, [ctypes.POINTER(vp), ctypes.POINTER(ServerConfig), u64]),
+        "fpa_server_submit_ex": (ctypes.c_int64, [vp, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp,
+                                                  ctypes.POINTER(ServerJobOpts)]),
+        "fpa_server_read": (i32, [vp, ctypes.c_int64, vp, vp]),
+        "fpa_server_costs": (i32, [vp, ctypes.POINTER(u64)]),
         "fpa_server_destroy": (i32, [vp]),
         "fpa_gb300_dot": (i32, [u32, u64, u32, i32, vp, vp, vp, vp, vp, vp, vp]),
         "fpa_gb300_newton_sqrt": (i32, [u32, u64, u32, i32, vp, vp, vp, vp, vp]),
@@ -363,31 +374,52 @@ class Server:
     """fpa_server_t: request loop with continuous batching (batching=True) or plain
     per-job launches (batching=False)."""
 
-    def __init__(self, hbm_budget_bytes=1 << 30, max_inflight=4, max_batch_ops=0, batching=True):
+    def __init__(self, hbm_budget_bytes=1 << 30, max_inflight=4, max_batch_ops=0, batching=True, resident_bytes=0):
         cfg = ServerConfig(hbm_budget_bytes, max_inflight, max_batch_ops, 1 if batching else 0)
         self.h = ctypes.c_void_p()
-        rc = lib().fpa_server_create(ctypes.byref(self.h), ctypes.byref(cfg))
+        rc = lib().fpa_server_create_resident(ctypes.byref(self.h), ctypes.byref(cfg), resident_bytes)
         if rc != fpa_success:
-            raise FpaError(f"fpa_server_create -> {rc}")
+            raise FpaError(f"fpa_server_create_resident -> {rc}")
         self._keep = {}
 
-    def submit(self, precision, ops, modes, a_exps, a_limbs, b_exps=None, b_limbs=None):
+    def submit(self, precision, ops, modes, a_exps, a_limbs, b_exps=None, b_limbs=None, a_from=0, b_from=0,
+               keep=False, copy_out=True):
         """Submit one job; returns (job_id, (r_exps, r_limbs)) whose arrays are filled when
-        the job completes."""
+        the job completes (None when copy_out is False).  a_from / b_from: job ids whose kept
+        results are the operands (the host operands are then ignored and may be None);
+        keep: keep this job's result on the device for later jobs and read()."""
         ops = np.ascontiguousarray(ops, dtype=np.uint8)
         count = ops.size
         modes = np.ascontiguousarray(modes, dtype=np.uint8) if modes is not None else None
         arrs = [np.ascontiguousarray(x, dtype=np.uint32) if x is not None else None
                 for x in (a_exps, a_limbs, b_exps, b_limbs)]
+        r_e = np.zeros(count, dtype=np.uint32) if copy_out else None
+        r_l = np.zeros(count * (precision // 32), dtype=np.uint32) if copy_out else None
+        p = lambda x: x.ctypes.data_as(ctypes.c_void_p) if x is not None else None
+        opts = ServerJobOpts(a_from, b_from, 1 if keep else 0, 1 if copy_out else 0)
+        jid = lib().fpa_server_submit_ex(self.h, precision, count, p(ops), p(modes), p(arrs[0]), p(arrs[1]),
+                                         p(arrs[2]), p(arrs[3]), p(r_e), p(r_l), ctypes.byref(opts))
+        if jid <= 0:
+            raise FpaError(f"fpa_server_submit_ex -> {-jid}")
+        self._keep[jid] = (ops, modes, arrs, r_e, r_l, precision, count)
+        return jid, (r_e, r_l)
+
+    def read(self, jid):
+        """A kept result, copied to host memory (waits for the job)."""
+        precision, count = self._keep[jid][5], self._keep[jid][6]
         r_e = np.zeros(count, dtype=np.uint32)
         r_l = np.zeros(count * (precision // 32), dtype=np.uint32)
-        p = lambda x: x.ctypes.data_as(ctypes.c_void_p) if x is not None else None
-        jid = lib().fpa_server_submit(self.h, precision, count, p(ops), p(modes), p(arrs[0]), p(arrs[1]),
-                                      p(arrs[2]), p(arrs[3]), p(r_e), p(r_l))
-        if jid <= 0:
-            raise FpaError(f"fpa_server_submit -> {-jid}")
-        self._keep[jid] = (ops, modes, arrs, r_e, r_l)
-        return jid, (r_e, r_l)
+        rc = lib().fpa_server_read(self.h, jid, r_e.ctypes.data_as(ctypes.c_void_p),
+                                   r_l.ctypes.data_as(ctypes.c_void_p))
+        if rc != fpa_success:
+            raise FpaError(f"fpa_server_read -> {rc}")
+        return r_e, r_l
+
+    def costs(self):
+        """Nanoseconds summed over all batches: host packing, host-to-device, kernels, device-to-host."""
+        c = (ctypes.c_uint64 * 4)()
+        lib().fpa_server_costs(self.h, c)
+        return dict(zip(["pack_ns", "h2d_ns", "device_ns", "d2h_ns"], list(c)))
 
     def wait(self, jid, timeout_ms=-1):
         return lib().fpa_server_wait(self.h, jid, timeout_ms)
@@ -398,8 +430,10 @@ class Server:
         return a.value, b.value, c.value
 
     def release(self, jid):
-        self._keep.pop(jid, None)
-        return lib().fpa_server_release(self.h, jid)
+        rc = lib().fpa_server_release(self.h, jid)
+        if rc == fpa_success:
+            self._keep.pop(jid, None)
+        return rc
 
     def stats(self):
         s = (ctypes.c_uint64 * 6)()

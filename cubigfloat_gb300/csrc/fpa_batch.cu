@@ -94,34 +94,53 @@ cudaError_t gfpa_batch_launch_class(int c, const BatchArgs *a, int grid, size_t 
   return launch(c, a, grid, smem, st);
 }
 
-fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan, bool one_thread) {
+fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan, bool one_thread,
+                           int thread_grid_cap) {
   if (count > 0xFFFFFFFFull) return fpa_invalid_counts;
   if (count && !descs) return fpa_math_error;
   std::vector<uint32_t> &order = plan.order;
   order.resize(count);
   std::vector<uint16_t> key(count);
   std::vector<uint8_t> cls(count);
+  // (key, class) of each (operation, limb count), worked out once per pair present
+  std::vector<int32_t> memo(5 * (GFPA_MAX_LIMBS + 1), -1);
+  std::vector<uint32_t> used;                             // memo entries in use
+  std::vector<uint32_t> slot(count);                      // each operation's memo entry
   for (uint64_t i = 0; i < count; i++) {
     const fpa_batch_desc &d = descs[i];
     if (d.op > 4 || d.mode > 4) return fpa_math_error;
     if (d.limbs == 0 || d.limbs > GFPA_MAX_LIMBS) return fpa_invalid_precisions;
-    order[i] = (uint32_t)i;
-    const int tcfg = one_thread && d.op >= OP_MUL && d.limbs >= 8 && d.limbs <= 128 ? gfpa_cfg_for_op(d.op, d.limbs) : -1;
-    if (tcfg == 18 || tcfg == 19) {                       // one thread per operation
-      key[i] = (uint16_t)(18 * 5 + d.op);
-      cls[i] = (uint8_t)GFPA_THREAD_CLASS;
-      continue;
+    const uint32_t me = d.op * (GFPA_MAX_LIMBS + 1) + d.limbs;
+    int32_t &m = memo[me];
+    if (m < 0) {
+      const int tcfg =
+          one_thread && d.op >= OP_MUL && d.limbs >= 8 && d.limbs <= 128 ? gfpa_cfg_for_op(d.op, d.limbs) : -1;
+      if (tcfg == 18 || tcfg == 19) {                     // one thread per operation
+        m = ((18 * 5 + d.op) << 8) | GFPA_THREAD_CLASS;
+      } else {
+        const int cfg = gfpa_batch_cfg_for(d.op, d.limbs);
+        if (cfg < 0) return fpa_invalid_precisions;
+        m = ((cfg * 5 + d.op) << 8) | gfpa_class_of(cfg, d.op);
+      }
+      used.push_back(me);
     }
-    const int cfg = gfpa_batch_cfg_for(d.op, d.limbs);
-    if (cfg < 0) return fpa_invalid_precisions;
-    key[i] = (uint16_t)(cfg * 5 + d.op);
-    cls[i] = (uint8_t)gfpa_class_of(cfg, d.op);
+    key[i] = (uint16_t)(m >> 8);
+    cls[i] = (uint8_t)(m & 0xFF);
+    slot[i] = me;
   }
-  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
-    if (cls[x] != cls[y]) return cls[x] < cls[y];
-    if (key[x] != key[y]) return key[x] < key[y];
-    return descs[x].limbs > descs[y].limbs;
+  // order by (class, configuration * 5 + operation, limbs descending, index): a counting sort
+  // over the (operation, limb count) pairs present, ranked by their (class, key, limbs)
+  std::sort(used.begin(), used.end(), [&](uint32_t x, uint32_t y) {
+    const int32_t mx = memo[x], my = memo[y];
+    if ((mx & 0xFF) != (my & 0xFF)) return (mx & 0xFF) < (my & 0xFF);
+    if ((mx >> 8) != (my >> 8)) return (mx >> 8) < (my >> 8);
+    return x % (GFPA_MAX_LIMBS + 1) > y % (GFPA_MAX_LIMBS + 1);
   });
+  std::vector<uint32_t> rank(memo.size(), 0), start(used.size() + 1, 0);
+  for (size_t k = 0; k < used.size(); k++) rank[used[k]] = (uint32_t)k;
+  for (uint64_t i = 0; i < count; i++) start[rank[slot[i]] + 1]++;
+  for (size_t k = 1; k < start.size(); k++) start[k] += start[k - 1];
+  for (uint64_t i = 0; i < count; i++) order[start[rank[slot[i]]]++] = (uint32_t)i;
   std::vector<BatchTask> tasks[4];
   std::vector<double> cost[4];
   uint64_t i = 0;
@@ -175,6 +194,7 @@ fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms,
         if (gfpa_batch_thread_prepare(&per) != cudaSuccess) return fpa_device_error;
         if (per < 1) per = 1;
         plan.grid[c] = (int)std::min<uint64_t>((uint64_t)per * sms, plan.ntasks[c]);
+        if (thread_grid_cap > 0) plan.grid[c] = std::min(plan.grid[c], thread_grid_cap);
       }
       continue;
     }

@@ -77,9 +77,10 @@ struct BatchPlan {
 };
 // Plan `count` descriptors; fpa_success or the validation error.  With `one_thread`, mul,
 // div and sqrt of 8 to 128 limbs whose tuned configuration is a one-thread one (18, 19) go to
-// the one-thread class, which needs a ThreadScratch at enqueue.
+// the one-thread class, which needs a ThreadScratch at enqueue with slabs for its grid (at
+// most `thread_grid_cap` CTAs when that is nonzero).
 fpa_result gfpa_batch_plan(const fpa_batch_desc *descs, uint64_t count, int sms, BatchPlan &plan,
-                           bool one_thread = false);
+                           bool one_thread = false, int thread_grid_cap = 0);
 // Enqueue one run of a plan whose descriptors, order and tasks are already in device memory.
 // Classes 0 and 3 run on `st`, classes 1 and 2 on `side[0]`, `side[1]` (forked from and
 // joined back into `st` with the given events).  `ts`: the one-thread class's scratch (only

@@ -145,6 +145,37 @@ fpa_result fpa_server_stats(fpa_server_t server, uint64_t *stats);
 /* Finish pending work and free everything. */
 fpa_result fpa_server_destroy(fpa_server_t server);
 
+/* Device-resident results (no counterpart in the reference).  A server created with a
+ * resident store keeps the results of jobs submitted with `keep` on the device until they
+ * are released, and a later job of the same precision and count may take either operand
+ * from such a result (`a_from` / `b_from` = its job id, the host operand pointers are then
+ * ignored).  The operand is copied device to device; while its source is still in flight
+ * the copy waits for it on the GPU, so a chain of jobs never returns to the host between
+ * steps.  A job waits in the queue until its sources are launched.  Batching servers only.
+ * The store is one device allocation of `resident_bytes`, made at creation; a job whose
+ * kept result does not fit is refused with -fpa_invalid_counts.  A source cannot be released
+ * while jobs that read it are pending. */
+typedef struct {
+  int64_t a_from;     /* > 0: operand a is that job's kept result */
+  int64_t b_from;     /* > 0: operand b is that job's kept result */
+  uint32_t keep;      /* 1: keep this job's result on the device */
+  uint32_t copy_out;  /* 1: also write the result to r_exps / r_limbs (0: they may be NULL) */
+} fpa_server_job_opts;
+fpa_result fpa_server_create_resident(fpa_server_t *server, const fpa_server_config *config,
+                                      uint64_t resident_bytes);
+/* fpa_server_submit with options (opts = NULL: the defaults of fpa_server_submit). */
+int64_t fpa_server_submit_ex(fpa_server_t server, uint32_t precision, uint32_t count, const uint8_t *ops,
+                             const uint8_t *modes, const uint32_t *a_exps, const uint32_t *a_limbs,
+                             const uint32_t *b_exps, const uint32_t *b_limbs, uint32_t *r_exps, uint32_t *r_limbs,
+                             const fpa_server_job_opts *opts);
+/* Copy a kept result to host memory (waits for the job). */
+fpa_result fpa_server_read(fpa_server_t server, int64_t job, uint32_t *r_exps, uint32_t *r_limbs);
+/* Cost account (no counterpart in the reference): ns[4] = nanoseconds summed over all batches
+ * of the server thread's packing and planning, the host-to-device copies (with kept-result
+ * operands), the kernels (with the copies into the resident store), and the device-to-host
+ * copy, the last three from CUDA events on each batch's stream. */
+fpa_result fpa_server_costs(fpa_server_t server, uint64_t *ns);
+
 /* Batched run without any memory allocation.  No counterpart in the reference.
  *
  * For callers that must not allocate GPU memory at the point where they compute: a serving

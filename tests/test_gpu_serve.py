@@ -112,3 +112,54 @@ def test_budget_rejects_oversized_job():
     jid, res = srv.submit(*small)
     assert srv.wait(jid, 60000) == 0 and same(oracle_job(small), res)
     srv.destroy()
+
+
+def test_device_resident_chain_matches_oracle():
+    """A chain of jobs whose operands are earlier jobs' kept results: x = a*b (kept, not
+    copied out), y = x + c (kept), z = y / a (copied out).  z is submitted right behind y, so
+    its source is still in flight when it is admitted (the copy waits on the GPU).  x cannot
+    be released while y is pending.  Every kept result read back, and z, equals the oracle's
+    step-by-step values, and the cost account has all four parts."""
+    n, count = 64, 300
+    prec = 32 * n
+    rng = np.random.default_rng(77)
+    ae, al = W.uniform(rng, count, n, -40, 40)
+    be, bl = W.uniform(rng, count, n, -40, 40)
+    ce, cl = W.uniform(rng, count, n, -40, 40)
+    modes = rng.integers(0, 5, size=count).astype(np.uint8)
+    off = np.arange(count, dtype=np.uint64) * n
+    lim = np.full(count, n, np.uint16)
+    step = lambda op, xe, xl, ye, yl: oracle.run_mixed(np.full(count, op, np.uint8), lim, modes, xe, xl, off,
+                                                       ye, yl, off, off, count * n, threads=8)
+    xe, xl = step(2, ae, al.ravel(), be, bl.ravel())
+    ye, yl = step(0, xe, xl, ce, cl.ravel())
+    ze, zl = step(3, ye, yl, ae, al.ravel())
+    srv = fpa.Server(hbm_budget_bytes=256 << 20, max_inflight=2, resident_bytes=64 << 20)
+    try:
+        j1, _ = srv.submit(prec, np.full(count, 2, np.uint8), modes, ae, al, be, bl, keep=True, copy_out=False)
+        assert srv.wait(j1, 60000) == 0
+        j2, _ = srv.submit(prec, np.zeros(count, np.uint8), modes, None, None, ce, cl, a_from=j1, keep=True,
+                           copy_out=False)
+        assert srv.release(j1) != 0                  # y, which reads x, is still pending
+        j3, (re3, rl3) = srv.submit(prec, np.full(count, 3, np.uint8), modes, None, None, ae, al, a_from=j2)
+        assert srv.wait(j3, 60000) == 0
+        assert same((xe, xl), srv.read(j1))
+        assert same((ye, yl), srv.read(j2))
+        assert same((ze, zl), (re3, rl3))
+        assert srv.release(j3) == 0 and srv.release(j2) == 0 and srv.release(j1) == 0
+        c = srv.costs()
+        assert all(v > 0 for v in c.values()), c
+    finally:
+        srv.destroy()
+
+
+def test_resident_store_full_is_refused():
+    n, count = 32, 1000
+    rng = np.random.default_rng(3)
+    ae, al = W.uniform(rng, count, n, -5, 5)
+    srv = fpa.Server(hbm_budget_bytes=64 << 20, max_inflight=1, resident_bytes=1 << 16)
+    try:
+        with pytest.raises(fpa.FpaError):
+            srv.submit(32 * n, np.full(count, 4, np.uint8), None, ae & ~np.uint32(1), al, keep=True)
+    finally:
+        srv.destroy()
