@@ -22,7 +22,7 @@ namespace gfpa {
 
 // One warp per CTA, and at least one CTA per SM requested from the compiler: shared memory
 // already limits a div/sqrt kernel to 9 warps per SM, and with this bound ptxas gives it the
-// registers it can use there (196-224 instead of 128; measured at 4096 bits: div 5.49 ->
+// registers it can use there (191-197 instead of 128; measured at 4096 bits: div 5.49 ->
 // 5.30 ms, sqrt 6.9 -> 5.7 ms per 2^20 operations).
 template <int OP, int N>
 __global__ void __launch_bounds__(32, 1) k_tnewton(ElementwiseArgs args, uint32_t *ctl, uint32_t *hard_idx,
