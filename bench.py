@@ -221,16 +221,24 @@ def mpfr_leg(data, gpu_results, threads, count=MPFR_SAMPLE):
 # The one-thread kernels (configuration 18: k_tmul, k_tnewton in fpa_thread_newton.cu) form
 # fewer limb products than the schoolbook basis counts: mul a short product above the
 # rounding limb, div and sqrt Newton levels and a Karp-Markstein step whose products are
-# restricted to the limbs that are read.  tile_products() mirrors their 8x8-tile block
-# ranges (tprod: output blocks [cb_lo, cb_hi) of an lx x ly product, block cb spanning
-# x blocks max(0, cb-My) .. min(cb, Mx-1)), so that the roofline can also report how busy
-# the multiplier is on the products the first pass executes (deferred operations excluded).
+# restricted to the limbs that are read, sqrt's square on its symmetric half.
+# tile_products() mirrors their 8x8-tile block ranges (tprod: output blocks [cb_lo, cb_hi)
+# of an lx x ly product, block cb spanning x blocks max(0, cb-My) .. min(cb, Mx-1); 64
+# products a tile, 36 for a div/sqrt edge tile whose window is half zero guard; tsqr: the
+# tiles below the diagonal), so that the roofline can also report how busy the multiplier is
+# on the products the first pass executes (deferred operations excluded).
 KERNELS = {"mul": "k_tmul<128>", "div": "k_tnewton<3 (div), 128>", "sqrt": "k_tnewton<4 (sqrt), 128>"}
 
 
-def _tprod_tiles(lx, ly, cb_lo, cb_hi):
+def _tprod(lx, ly, cb_lo, cb_hi, edge=True):
     mx, my = (lx + 7) // 8, (ly + 7) // 8
-    return sum(min(cb, mx - 1) - max(0, cb - my) + 1 for cb in range(cb_lo, min(mx + my, cb_hi)))
+    total = 0
+    for cb in range(cb_lo, min(mx + my, cb_hi)):
+        i1 = min(cb, mx - 1)
+        total += 64 * (i1 - max(0, cb - my) + 1)
+        if edge:
+            total -= (28 if cb >= my else 0) + (28 if i1 == cb else 0)
+    return total
 
 
 def _levels(n):
@@ -242,42 +250,54 @@ def _levels(n):
     return out[::-1]
 
 
+def _tsqr(lx, cb_hi):
+    """Limb products of tsqr (x*x, output blocks [0, cb_hi)): the tiles below the diagonal
+    tile once (doubled afterwards), the diagonal tile's a < b pairs (16 for even blocks, 48
+    for odd) and its 4 squares."""
+    mx = (lx + 7) // 8
+    total = 0
+    for cb in range(0, min(2 * mx, cb_hi)):
+        i0, d = max(0, cb - mx), cb // 2
+        total += 64 * (d - i0) - (28 if (cb >= mx and i0 < d) else 0) + (52 if cb & 1 else 20)
+    return total
+
+
 def tile_products(op, n):
     """Limb products (64 per 8x8 tile) of the first pass of one operation at n limbs."""
     blk = lambda keep: max(0, keep - 2) // 8
     big = 1 << 20
     if op == "mul":
-        return 64 * _tprod_tiles(n, n, blk(n - 1), big)
+        return _tprod(n, n, blk(n - 1), big, edge=False)   # mul's short product keeps whole edge tiles
     lv = _levels(n)
     e = 1
     while e < len(lv) - 1 and lv[e] <= 9:          # one-thread register levels
         e += 1
-    tiles = 0
+    prods = 0
     for li in range(e, len(lv) - 1):
         k, kp = lv[li - 1], lv[li]
         lt = kp - k + 3
         if op == "div":
-            tiles += _tprod_tiles(kp, k + 1, blk(k - 1), (k + kp) // 8 + 1)
-            tiles += _tprod_tiles(k + 1, lt, blk(k + 1), (k + 1 + lt + 7) // 8)
+            prods += _tprod(kp, k + 1, blk(k - 1), (k + kp) // 8 + 1)
+            prods += _tprod(k + 1, lt, blk(k + 1), (k + 1 + lt + 7) // 8)
         else:
             j = k - 2 if k > 2 else 0
             l1, L, off = kp + k + 1 - j, kp + 2 * k - j, 2 * k - 1 - j
-            tiles += _tprod_tiles(kp, k + 1, blk(j), (j + l1 + 7) // 8)
-            tiles += _tprod_tiles(l1, k + 1, blk(off), L // 8 + 1)
-            tiles += _tprod_tiles(k + 1, lt, blk(k + 1), big)
+            prods += _tprod(kp, k + 1, blk(j), (j + l1 + 7) // 8)
+            prods += _tprod(l1, k + 1, blk(off), L // 8 + 1)
+            prods += _tprod(k + 1, lt, blk(k + 1), big)
     h = lv[-2]
     m = n + 2 - h
     if op == "div":
         dlen, sh = m + 2, n - h - 1
-        tiles += _tprod_tiles(m + 1, h + 1, blk(h + 1), (h + m + 9) // 8)
-        tiles += _tprod_tiles(m + 1, n, blk(sh), (sh + dlen + 7) // 8)
-        tiles += _tprod_tiles(dlen, h + 1, blk(h + 2), (dlen + h + 8) // 8)
+        prods += _tprod(m + 1, h + 1, blk(h + 1), (h + m + 9) // 8)
+        prods += _tprod(m + 1, n, blk(sh), (sh + dlen + 7) // 8)
+        prods += _tprod(dlen, h + 1, blk(h + 2), (dlen + h + 8) // 8)
     else:
         dlen, ssh = m + 3, 2 * h - n
-        tiles += _tprod_tiles(m + 1, h + 1, blk(h + 1), (h + m + 9) // 8)
-        tiles += _tprod_tiles(m + 1, m + 1, 0, (dlen - ssh + 7) // 8)
-        tiles += _tprod_tiles(dlen, h + 1, blk(h + 3), big)
-    return 64 * tiles
+        prods += _tprod(m + 1, h + 1, blk(h + 1), (h + m + 9) // 8)
+        prods += _tsqr(m + 1, (dlen - ssh + 7) // 8)
+        prods += _tprod(dlen, h + 1, blk(h + 3), big)
+    return prods
 
 
 def load_traffic():

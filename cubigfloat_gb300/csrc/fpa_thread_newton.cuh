@@ -47,6 +47,7 @@
 // limbs contiguous).  Reference semantics as op_div / op_sqrt: fpa_warp_div.h:127-201,
 // fpa_warp_sqrt.h:195-254.
 #pragma once
+#include <type_traits>
 #include "fpa_ops.cuh"
 
 namespace gfpa {
@@ -110,7 +111,28 @@ __device__ __forceinline__ void zero_tail(uint32_t *p, int len) {
 // sink(cb, L) receives limbs 8cb .. 8cb+7 in L[0..7].  NEXT: the next block's first-tile
 // operands load while the current block computes (24 more live registers: a gain for mul's
 // kernel, a loss where registers are already scarce, as in div and sqrt).
-template <bool NEXT = false, class X, class Y, class Sink>
+//
+// EDGE: a block's first tile reads its window's upper half from y's zero guard when
+// cb >= My, and its last tile (i = cb) reads the lower half from the guard below y; the 28
+// products of such a half are skipped (MASK 1 keeps column c of row r only for c < r,
+// MASK 2 only for c >= r).  Measured at 4096 bits: div 5.30 -> 5.16 ms and sqrt 5.71 ->
+// 5.51 ms per 2^20 operations, but mul's short product (NEXT) 2.03 -> 2.70 ms, so mul
+// keeps the plain loop.
+
+// one 8x8 tile: column c gathers a[r] * w[8 + c - r]
+template <int MASK>
+__device__ __forceinline__ void tile_mac(uint32_t (&lo)[8], uint32_t (&hi)[8], uint32_t (&tp)[8], const uint32_t (&a)[8],
+                                         const uint32_t (&w)[16]) {
+#pragma unroll
+  for (int r = 0; r < 8; r++)
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+      if (MASK == 0 || (MASK == 1 && c < r) || (MASK == 2 && c >= r) || (MASK == 3 && 2 * r < c) ||
+          (MASK == 4 && 2 * r - c < 8))
+        mac3(lo[c], hi[c], tp[c], a[r], w[8 + c - r]);
+}
+
+template <bool NEXT = false, bool EDGE = true, class X, class Y, class Sink>
 __device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, int cb_lo, int cb_hi, Sink &&sink) {
   const int Mx = (lx + 7) >> 3, My = (ly + 7) >> 3;
   const int Mo = min(Mx + My, cb_hi);
@@ -147,22 +169,107 @@ __device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, in
 #pragma unroll
       for (int m = 0; m < 16; m++) w[m] = y.get(8 * (cb - i0) - 8 + m);
     }
-#pragma unroll 2
-    for (int i = i0; i <= i1; i++) {
-      uint32_t an[8], wn[8];              // the next tile's operands, loaded ahead of the math
+    // the next tile's operands load ahead of the math
+    auto step = [&](int i, auto mask) {
+      uint32_t an[8], wn[8];
 #pragma unroll
       for (int r = 0; r < 8; r++) an[r] = x.get(8 * (i + 1) + r);
 #pragma unroll
       for (int m = 0; m < 8; m++) wn[m] = y.get(8 * (cb - i - 2) + m);
-#pragma unroll
-      for (int r = 0; r < 8; r++)
-#pragma unroll
-        for (int c = 0; c < 8; c++) mac3(lo[c], hi[c], tp[c], a[r], w[8 + c - r]);
+      tile_mac<decltype(mask)::value>(lo, hi, tp, a, w);
 #pragma unroll
       for (int r = 0; r < 8; r++) a[r] = an[r];
 #pragma unroll
       for (int m = 0; m < 8; m++) { w[8 + m] = w[m]; w[m] = wn[m]; }
+    };
+    if constexpr (EDGE) {
+      int i = i0;
+      if (cb >= My) step(i++, std::integral_constant<int, 1>{});   // upper window half in the guard
+      const int iend = i1 == cb ? i1 : i1 + 1;                       // i = cb: lower half in the guard
+#pragma unroll 2
+      for (; i < iend; i++) step(i, std::integral_constant<int, 0>{});
+      if (i1 == cb) tile_mac<2>(lo, hi, tp, a, w);
+    } else {
+#pragma unroll 2
+      for (int i = i0; i <= i1; i++) {
+        uint32_t an[8], wn[8];
+#pragma unroll
+        for (int r = 0; r < 8; r++) an[r] = x.get(8 * (i + 1) + r);
+#pragma unroll
+        for (int m = 0; m < 8; m++) wn[m] = y.get(8 * (cb - i - 2) + m);
+#pragma unroll
+        for (int r = 0; r < 8; r++)
+#pragma unroll
+          for (int c = 0; c < 8; c++) mac3(lo[c], hi[c], tp[c], a[r], w[8 + c - r]);
+#pragma unroll
+        for (int r = 0; r < 8; r++) a[r] = an[r];
+#pragma unroll
+        for (int m = 0; m < 8; m++) { w[8 + m] = w[m]; w[m] = wn[m]; }
+      }
     }
+    uint32_t L[10];
+    columns_to_limbs<8>(lo, hi, tp, L);
+    sink(cb, L);
+    c0 = L[8]; c1 = L[9];
+  }
+}
+
+// ---- square: output blocks [0, cb_hi) of x * x -------------------------------------------
+// The tiles of tprod(x, x) pair limbs a (x-block i) and b = 8(cb-i) + c - r.  In block cb,
+// the tiles with i < floor(cb/2) hold only pairs a < b and are summed once, then doubled;
+// those with i > cb/2 hold only their mirror images (a > b) and are skipped.  The tile
+// i = floor(cb/2) holds both and a = b: MASK 3 (even cb) or 4 (odd cb) keeps its a < b
+// pairs before the doubling, the squares x_a^2 are added after it, then the carry from the
+// block below.  About half of tprod's products.
+template <class X, class Sink>
+__device__ __forceinline__ void tsqr(const X &x, int lx, int cb_hi, Sink &&sink) {
+  const int Mx = (lx + 7) >> 3;
+  const int Mo = min(2 * Mx, cb_hi);
+  uint32_t c0 = 0u, c1 = 0u;
+#pragma unroll 1
+  for (int cb = 0; cb < Mo; cb++) {
+    uint32_t lo[8], hi[8], tp[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) { lo[c] = 0u; hi[c] = 0u; tp[c] = 0u; }
+    const int i0 = max(0, cb - Mx), id = cb >> 1;
+    uint32_t a[8], w[16];
+#pragma unroll
+    for (int r = 0; r < 8; r++) a[r] = x.get(8 * i0 + r);
+#pragma unroll
+    for (int m = 0; m < 16; m++) w[m] = x.get(8 * (cb - i0) - 8 + m);
+    auto step = [&](int i, auto mask) {
+      uint32_t an[8], wn[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++) an[r] = x.get(8 * (i + 1) + r);
+#pragma unroll
+      for (int m = 0; m < 8; m++) wn[m] = x.get(8 * (cb - i - 2) + m);
+      tile_mac<decltype(mask)::value>(lo, hi, tp, a, w);
+#pragma unroll
+      for (int r = 0; r < 8; r++) a[r] = an[r];
+#pragma unroll
+      for (int m = 0; m < 8; m++) { w[8 + m] = w[m]; w[m] = wn[m]; }
+    };
+    int i = i0;
+    if (i < id && cb >= Mx) step(i++, std::integral_constant<int, 1>{});   // upper window half in the guard
+#pragma unroll 2
+    for (; i < id; i++) step(i, std::integral_constant<int, 0>{});
+    if (cb & 1) tile_mac<4>(lo, hi, tp, a, w);
+    else tile_mac<3>(lo, hi, tp, a, w);
+#pragma unroll
+    for (int c = 0; c < 8; c++) {                     // double the (top, hi, lo) column sums
+      tp[c] = (tp[c] << 1) | (hi[c] >> 31);
+      hi[c] = (hi[c] << 1) | (lo[c] >> 31);
+      lo[c] <<= 1;
+    }
+    if (cb & 1) {                                     // x_a^2 lands in column 2a - 8cb
+#pragma unroll
+      for (int r = 4; r < 8; r++) mac3(lo[2 * r - 8], hi[2 * r - 8], tp[2 * r - 8], a[r], a[r]);
+    } else {
+#pragma unroll
+      for (int r = 0; r < 4; r++) mac3(lo[2 * r], hi[2 * r], tp[2 * r], a[r], a[r]);
+    }
+    mac3(lo[0], hi[0], tp[0], c0, 1u);
+    mac3(lo[1], hi[1], tp[1], c1, 1u);
     uint32_t L[10];
     columns_to_limbs<8>(lo, hi, tp, L);
     sink(cb, L);
@@ -550,7 +657,7 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
     bw = (xs < ss || (xs == ss && bw)) ? 1u : 0u;
   };
   for (int i = 0; i < ssh; i++) putd(i, 0u);
-  tprod(PV{S0}, m + 1, PV{S0}, m + 1, 0, (dlen - ssh + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
+  tsqr(PV{S0}, m + 1, (dlen - ssh + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q + ssh;
@@ -622,7 +729,7 @@ __device__ int tsqrt(uint32_t *w, uint32_t *slab, int n, int mode, uint32_t a_ex
   };
   int nextr = 0;
   const VW sl{Sc, n};
-  tprod(sl, n, sl, n, 0, (n + 2 + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
+  tsqr(sl, n, (n + 2 + 7) / 8, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int i = 8 * cb + q;
@@ -724,7 +831,7 @@ __device__ __forceinline__ int tmul_op(uint32_t *A, uint32_t *B, uint32_t *Q, in
   const int cb0 = exact ? 0 : blk(n - 1), c0 = 8 * cb0;
   uint32_t low = 0u;                                   // exact: OR of limbs 0 .. n-2
   uint32_t l1 = 0u, midz = 0u, mido = 0xFFFFFFFFu;     // short: limb c0+1; OR / AND of limbs c0+2 .. n-2
-  tprod<true>(PV{A}, n, PV{B}, n, cb0, 1 << 20, [&](int cb, const uint32_t (&o)[10]) {
+  tprod<true, false>(PV{A}, n, PV{B}, n, cb0, 1 << 20, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int p = 8 * cb + q;
