@@ -224,20 +224,19 @@ def mpfr_leg(data, gpu_results, threads, count=MPFR_SAMPLE):
 # restricted to the limbs that are read, sqrt's square on its symmetric half.
 # tile_products() mirrors their 8x8-tile block ranges (tprod: output blocks [cb_lo, cb_hi)
 # of an lx x ly product, block cb spanning x blocks max(0, cb-My) .. min(cb, Mx-1); 64
-# products a tile, 36 for a div/sqrt edge tile whose window is half zero guard; tsqr: the
-# tiles below the diagonal), so that the roofline can also report how busy the multiplier is
-# on the products the first pass executes (deferred operations excluded).
+# products a tile, 36 for an edge tile whose window is half zero guard; tprod2, mul's: two
+# blocks per pass; tsqr: the tiles below the diagonal), so that the roofline can also report
+# how busy the multiplier is on the products the first pass executes (deferred operations
+# excluded).
 KERNELS = {"mul": "k_tmul<128>", "div": "k_tnewton<3 (div), 128>", "sqrt": "k_tnewton<4 (sqrt), 128>"}
 
 
-def _tprod(lx, ly, cb_lo, cb_hi, edge=True):
+def _tprod(lx, ly, cb_lo, cb_hi):
     mx, my = (lx + 7) // 8, (ly + 7) // 8
     total = 0
     for cb in range(cb_lo, min(mx + my, cb_hi)):
         i1 = min(cb, mx - 1)
-        total += 64 * (i1 - max(0, cb - my) + 1)
-        if edge:
-            total -= (28 if cb >= my else 0) + (28 if i1 == cb else 0)
+        total += 64 * (i1 - max(0, cb - my) + 1) - (28 if cb >= my else 0) - (28 if i1 == cb else 0)
     return total
 
 
@@ -248,6 +247,21 @@ def _levels(n):
         k = k - 1 if p >= k else p
         out.append(k)
     return out[::-1]
+
+
+def _tprod2(lx, ly, cb_lo, cb_hi):
+    """Limb products of tprod2 (two output blocks per pass): 128 per tile of both blocks, 28
+    and 36 for the lone half tiles, 64 per tile of a last unpaired block."""
+    mx, my = (lx + 7) // 8, (ly + 7) // 8
+    mo, cb, total = min(mx + my, cb_hi), cb_lo, 0
+    while cb + 1 < mo:
+        i0a, i1a = max(0, cb - my), min(cb, mx - 1)
+        i0b, i1b = max(0, cb + 1 - my), min(cb + 1, mx - 1)
+        total += (28 if i0a < i0b else 0) + 128 * (i1a - i0b + 1) + (36 if i1b > i1a else 0)
+        cb += 2
+    if cb < mo:
+        total += 64 * (min(cb, mx - 1) - max(0, cb - my) + 1)
+    return total
 
 
 def _tsqr(lx, cb_hi):
@@ -267,7 +281,7 @@ def tile_products(op, n):
     blk = lambda keep: max(0, keep - 2) // 8
     big = 1 << 20
     if op == "mul":
-        return _tprod(n, n, blk(n - 1), big, edge=False)   # mul's short product keeps whole edge tiles
+        return _tprod2(n, n, blk(n - 1), big)
     lv = _levels(n)
     e = 1
     while e < len(lv) - 1 and lv[e] <= 9:          # one-thread register levels

@@ -108,43 +108,33 @@ __device__ __forceinline__ void zero_tail(uint32_t *p, int len) {
 // Output block cb gathers x-block i times the y window y[8(cb-i)-8 .. 8(cb-i)+7] for every i
 // with 0 <= cb-i <= My (My = y's block count), into 96-bit (lo, hi, top) column sums fed by
 // mac3; the two limbs above a block carry into the next one (none into block cb_lo).
-// sink(cb, L) receives limbs 8cb .. 8cb+7 in L[0..7].  NEXT: the next block's first-tile
-// operands load while the current block computes (24 more live registers: a gain for mul's
-// kernel, a loss where registers are already scarce, as in div and sqrt).
+// sink(cb, L) receives limbs 8cb .. 8cb+7 in L[0..7].
 //
-// EDGE: a block's first tile reads its window's upper half from y's zero guard when
-// cb >= My, and its last tile (i = cb) reads the lower half from the guard below y; the 28
-// products of such a half are skipped (MASK 1 keeps column c of row r only for c < r,
-// MASK 2 only for c >= r).  Measured at 4096 bits: div 5.30 -> 5.16 ms and sqrt 5.71 ->
-// 5.51 ms per 2^20 operations, but mul's short product (NEXT) 2.03 -> 2.70 ms, so mul
-// keeps the plain loop.
+// A block's first tile reads its window's upper half from y's zero guard when cb >= My, and
+// its last tile (i = cb) reads the lower half from the guard below y; the 28 products of
+// such a half are skipped (MASK 1 keeps column c of row r only for c < r, MASK 2 only for
+// c >= r).  Measured at 4096 bits: div 5.30 -> 5.16 ms and sqrt 5.71 -> 5.51 ms per 2^20
+// operations.  (Loading the next block's first tile during the current block cost div and
+// sqrt registers they lack; mul's short product runs on tprod2 below.)
 
-// one 8x8 tile: column c gathers a[r] * w[8 + c - r]
-template <int MASK>
+// one 8x8 tile: column c gathers a[r] * w[OFF + 8 + c - r]
+template <int MASK, int OFF = 0, int W>
 __device__ __forceinline__ void tile_mac(uint32_t (&lo)[8], uint32_t (&hi)[8], uint32_t (&tp)[8], const uint32_t (&a)[8],
-                                         const uint32_t (&w)[16]) {
+                                         const uint32_t (&w)[W]) {
 #pragma unroll
   for (int r = 0; r < 8; r++)
 #pragma unroll
     for (int c = 0; c < 8; c++)
       if (MASK == 0 || (MASK == 1 && c < r) || (MASK == 2 && c >= r) || (MASK == 3 && 2 * r < c) ||
           (MASK == 4 && 2 * r - c < 8))
-        mac3(lo[c], hi[c], tp[c], a[r], w[8 + c - r]);
+        mac3(lo[c], hi[c], tp[c], a[r], w[OFF + 8 + c - r]);
 }
 
-template <bool NEXT = false, bool EDGE = true, class X, class Y, class Sink>
+template <class X, class Y, class Sink>
 __device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, int cb_lo, int cb_hi, Sink &&sink) {
   const int Mx = (lx + 7) >> 3, My = (ly + 7) >> 3;
   const int Mo = min(Mx + My, cb_hi);
   uint32_t c0 = 0u, c1 = 0u;
-  uint32_t a0[8], w0[16];
-  if (NEXT) {
-    const int i0 = max(0, cb_lo - My);
-#pragma unroll
-    for (int r = 0; r < 8; r++) a0[r] = x.get(8 * i0 + r);
-#pragma unroll
-    for (int m = 0; m < 16; m++) w0[m] = y.get(8 * (cb_lo - i0) - 8 + m);
-  }
 #pragma unroll 1
   for (int cb = cb_lo; cb < Mo; cb++) {
     uint32_t lo[8], hi[8], tp[8];
@@ -153,22 +143,10 @@ __device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, in
     lo[0] = c0; lo[1] = c1;
     const int i0 = max(0, cb - My), i1 = min(cb, Mx - 1);
     uint32_t a[8], w[16];
-    if (NEXT) {
 #pragma unroll
-      for (int r = 0; r < 8; r++) a[r] = a0[r];
+    for (int r = 0; r < 8; r++) a[r] = x.get(8 * i0 + r);
 #pragma unroll
-      for (int m = 0; m < 16; m++) w[m] = w0[m];
-      const int j0 = max(0, cb + 1 - My);   // block cb+1's first tile (read past the end on the last block)
-#pragma unroll
-      for (int r = 0; r < 8; r++) a0[r] = x.get(8 * j0 + r);
-#pragma unroll
-      for (int m = 0; m < 16; m++) w0[m] = y.get(8 * (cb + 1 - j0) - 8 + m);
-    } else {
-#pragma unroll
-      for (int r = 0; r < 8; r++) a[r] = x.get(8 * i0 + r);
-#pragma unroll
-      for (int m = 0; m < 16; m++) w[m] = y.get(8 * (cb - i0) - 8 + m);
-    }
+    for (int m = 0; m < 16; m++) w[m] = y.get(8 * (cb - i0) - 8 + m);
     // the next tile's operands load ahead of the math
     auto step = [&](int i, auto mask) {
       uint32_t an[8], wn[8];
@@ -182,35 +160,112 @@ __device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, in
 #pragma unroll
       for (int m = 0; m < 8; m++) { w[8 + m] = w[m]; w[m] = wn[m]; }
     };
-    if constexpr (EDGE) {
-      int i = i0;
-      if (cb >= My) step(i++, std::integral_constant<int, 1>{});   // upper window half in the guard
-      const int iend = i1 == cb ? i1 : i1 + 1;                       // i = cb: lower half in the guard
+    int i = i0;
+    if (cb >= My) step(i++, std::integral_constant<int, 1>{});   // upper window half in the guard
+    const int iend = i1 == cb ? i1 : i1 + 1;                       // i = cb: lower half in the guard
 #pragma unroll 2
-      for (; i < iend; i++) step(i, std::integral_constant<int, 0>{});
-      if (i1 == cb) tile_mac<2>(lo, hi, tp, a, w);
-    } else {
-#pragma unroll 2
-      for (int i = i0; i <= i1; i++) {
-        uint32_t an[8], wn[8];
-#pragma unroll
-        for (int r = 0; r < 8; r++) an[r] = x.get(8 * (i + 1) + r);
-#pragma unroll
-        for (int m = 0; m < 8; m++) wn[m] = y.get(8 * (cb - i - 2) + m);
-#pragma unroll
-        for (int r = 0; r < 8; r++)
-#pragma unroll
-          for (int c = 0; c < 8; c++) mac3(lo[c], hi[c], tp[c], a[r], w[8 + c - r]);
-#pragma unroll
-        for (int r = 0; r < 8; r++) a[r] = an[r];
-#pragma unroll
-        for (int m = 0; m < 8; m++) { w[8 + m] = w[m]; w[m] = wn[m]; }
-      }
-    }
+    for (; i < iend; i++) step(i, std::integral_constant<int, 0>{});
+    if (i1 == cb) tile_mac<2>(lo, hi, tp, a, w);
     uint32_t L[10];
     columns_to_limbs<8>(lo, hi, tp, L);
     sink(cb, L);
     c0 = L[8]; c1 = L[9];
+  }
+}
+
+// ---- product, two output blocks per pass --------------------------------------------------
+// The result of tprod, with blocks cb and cb+1 formed together: tile i of block cb+1 reads
+// the y window 8 limbs above that of block cb, so one 24-limb window
+// u = y[8(cb-i)-8 .. 8(cb-i)+15] serves both, each new 8 y limbs feed 128 products, and the
+// two blocks' column sums are independent chains.  Block cb's first tile when cb >= My and
+// block cb+1's last tile (i = cb+1) run alone, on their nonzero half; tiles of both blocks
+// run whole.  Block cb+1 takes block cb's carry after its sums are formed.  A last unpaired
+// block runs with whole tiles.  Measured at 4096 bits: mul's short product 2.03 -> 1.86 ms
+// per 2^20 operations; div and sqrt (230 instead of about 200 registers, 8 warps per SM
+// instead of 9) 5.15 -> 5.97 and 5.36 -> 6.41 ms, so they keep tprod.
+template <class X, class Y, class Sink>
+__device__ __forceinline__ void tprod2(const X &x, int lx, const Y &y, int ly, int cb_lo, int cb_hi, Sink &&sink) {
+  const int Mx = (lx + 7) >> 3, My = (ly + 7) >> 3;
+  const int Mo = min(Mx + My, cb_hi);
+  uint32_t c0 = 0u, c1 = 0u;
+  int cb = cb_lo;
+  using I0 = std::integral_constant<int, 0>;
+#pragma unroll 1
+  for (; cb + 1 < Mo; cb += 2) {
+    uint32_t lo[8], hi[8], tp[8], lo2[8], hi2[8], tp2[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) { lo[c] = 0u; hi[c] = 0u; tp[c] = 0u; lo2[c] = 0u; hi2[c] = 0u; tp2[c] = 0u; }
+    lo[0] = c0; lo[1] = c1;
+    const int i0a = max(0, cb - My), i1a = min(cb, Mx - 1);
+    const int i0b = max(0, cb + 1 - My), i1b = min(cb + 1, Mx - 1);
+    uint32_t a[8], u[24];
+#pragma unroll
+    for (int r = 0; r < 8; r++) a[r] = x.get(8 * i0a + r);
+#pragma unroll
+    for (int m = 0; m < 24; m++) u[m] = y.get(8 * (cb - i0a) - 8 + m);
+    // kind 0: both blocks, 1: block cb alone (upper half of its window in the guard)
+    auto step = [&](int i, auto kind) {
+      uint32_t an[8], un[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++) an[r] = x.get(8 * (i + 1) + r);
+#pragma unroll
+      for (int m = 0; m < 8; m++) un[m] = y.get(8 * (cb - i - 2) + m);
+      constexpr int K = decltype(kind)::value;
+      if constexpr (K == 0) {
+        tile_mac<0, 0>(lo, hi, tp, a, u);
+        tile_mac<0, 8>(lo2, hi2, tp2, a, u);
+      } else {
+        tile_mac<1, 0>(lo, hi, tp, a, u);
+      }
+#pragma unroll
+      for (int r = 0; r < 8; r++) a[r] = an[r];
+#pragma unroll
+      for (int m = 23; m >= 8; m--) u[m] = u[m - 8];
+#pragma unroll
+      for (int m = 0; m < 8; m++) u[m] = un[m];
+    };
+    int i = i0a;
+    if (i0a < i0b) step(i++, std::integral_constant<int, 1>{});
+#pragma unroll 2
+    for (; i <= i1a; i++) step(i, I0{});
+    // block cb+1 alone at i = cb+1 (lower half of its window in the guard; no next tile to load)
+    if (i1b > i1a) tile_mac<2, 8>(lo2, hi2, tp2, a, u);
+    uint32_t L[10];
+    columns_to_limbs<8>(lo, hi, tp, L);
+    sink(cb, L);
+    mac3(lo2[0], hi2[0], tp2[0], L[8], 1u);
+    mac3(lo2[1], hi2[1], tp2[1], L[9], 1u);
+    columns_to_limbs<8>(lo2, hi2, tp2, L);
+    sink(cb + 1, L);
+    c0 = L[8]; c1 = L[9];
+  }
+  if (cb < Mo) {
+    uint32_t lo[8], hi[8], tp[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) { lo[c] = 0u; hi[c] = 0u; tp[c] = 0u; }
+    lo[0] = c0; lo[1] = c1;
+    const int i0 = max(0, cb - My), i1 = min(cb, Mx - 1);
+    uint32_t a[8], w[16];
+#pragma unroll
+    for (int r = 0; r < 8; r++) a[r] = x.get(8 * i0 + r);
+#pragma unroll
+    for (int m = 0; m < 16; m++) w[m] = y.get(8 * (cb - i0) - 8 + m);
+#pragma unroll 1
+    for (int i = i0; i <= i1; i++) {
+      uint32_t an[8], wn[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++) an[r] = x.get(8 * (i + 1) + r);
+#pragma unroll
+      for (int m = 0; m < 8; m++) wn[m] = y.get(8 * (cb - i - 2) + m);
+      tile_mac<0>(lo, hi, tp, a, w);
+#pragma unroll
+      for (int r = 0; r < 8; r++) a[r] = an[r];
+#pragma unroll
+      for (int m = 0; m < 8; m++) { w[8 + m] = w[m]; w[m] = wn[m]; }
+    }
+    uint32_t L[10];
+    columns_to_limbs<8>(lo, hi, tp, L);
+    sink(cb, L);
   }
 }
 
@@ -831,7 +886,7 @@ __device__ __forceinline__ int tmul_op(uint32_t *A, uint32_t *B, uint32_t *Q, in
   const int cb0 = exact ? 0 : blk(n - 1), c0 = 8 * cb0;
   uint32_t low = 0u;                                   // exact: OR of limbs 0 .. n-2
   uint32_t l1 = 0u, midz = 0u, mido = 0xFFFFFFFFu;     // short: limb c0+1; OR / AND of limbs c0+2 .. n-2
-  tprod<true, false>(PV{A}, n, PV{B}, n, cb0, 1 << 20, [&](int cb, const uint32_t (&o)[10]) {
+  tprod2(PV{A}, n, PV{B}, n, cb0, 1 << 20, [&](int cb, const uint32_t (&o)[10]) {
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const int p = 8 * cb + q;
