@@ -103,7 +103,8 @@ def extract(src, start, end):
     return src[a:b]
 
 
-def host_source():
+def host_body():
+    """The host-compiled device code (shims, then the extracted functions), without a main."""
     dev = open(os.path.join(CSRC, "fpa_device.cuh")).read()
     ops = open(os.path.join(CSRC, "fpa_ops.cuh")).read()
     tn = open(os.path.join(CSRC, "fpa_thread_newton.cuh")).read()
@@ -127,7 +128,11 @@ def host_source():
     body = re.sub(r"__device__\s+__noinline__", "", body)
     body = re.sub(r"__device__", "", body)
     body = re.sub(r"#pragma unroll[^\n]*", "", body)
-    return SHIMS + body + MAIN
+    return SHIMS + body
+
+
+def host_source():
+    return host_body() + MAIN
 
 
 @pytest.fixture(scope="module")
