@@ -224,7 +224,8 @@ def mpfr_leg(data, gpu_results, threads, count=MPFR_SAMPLE):
 # restricted to the limbs that are read, sqrt's square on its symmetric half.
 # tile_products() mirrors their 8x8-tile block ranges (tprod: output blocks [cb_lo, cb_hi)
 # of an lx x ly product, block cb spanning x blocks max(0, cb-My) .. min(cb, Mx-1); 64
-# products a tile, 36 for an edge tile whose window is half zero guard; tprod2, mul's: two
+# products a tile, 36 for an edge tile whose window is half zero guard, 32 for a tile of x's
+# last block when it holds 1 to 4 limbs; tprod2, mul's: two
 # blocks per pass; tsqr: the tiles below the diagonal), so that the roofline can also report
 # how busy the multiplier is on the products the first pass executes (deferred operations
 # excluded).
@@ -233,10 +234,14 @@ KERNELS = {"mul": "k_tmul<128>", "div": "k_tnewton<3 (div), 128>", "sqrt": "k_tn
 
 def _tprod(lx, ly, cb_lo, cb_hi):
     mx, my = (lx + 7) // 8, (ly + 7) // 8
+    half_rows = 0 < lx % 8 <= 4
     total = 0
     for cb in range(cb_lo, min(mx + my, cb_hi)):
-        i1 = min(cb, mx - 1)
-        total += 64 * (i1 - max(0, cb - my) + 1) - (28 if cb >= my else 0) - (28 if i1 == cb else 0)
+        i0, i1 = max(0, cb - my), min(cb, mx - 1)
+        total += 64 * (i1 - i0 + 1) - (28 if cb >= my else 0) - (28 if i1 == cb else 0)
+        iend, i = (i1 if i1 == cb else i1 + 1), i0 + (1 if cb >= my else 0)
+        if half_rows and iend == mx and i < iend:      # x's last block, rows 4..7 zero
+            total -= 32
     return total
 
 

@@ -114,7 +114,8 @@ __device__ __forceinline__ void zero_tail(uint32_t *p, int len) {
 // its last tile (i = cb) reads the lower half from the guard below y; the 28 products of
 // such a half are skipped (MASK 1 keeps column c of row r only for c < r, MASK 2 only for
 // c >= r).  Measured at 4096 bits: div 5.30 -> 5.16 ms and sqrt 5.71 -> 5.51 ms per 2^20
-// operations.  (Loading the next block's first tile during the current block cost div and
+// operations.  When x's last block holds 1 to 4 limbs, its rows 4..7 are zero guard: a
+// tile of that block that is not an edge tile skips them (MASK 5).  (Loading the next block's first tile during the current block cost div and
 // sqrt registers they lack; mul's short product runs on tprod2 below.)
 
 // one 8x8 tile: column c gathers a[r] * w[OFF + 8 + c - r]
@@ -126,7 +127,7 @@ __device__ __forceinline__ void tile_mac(uint32_t (&lo)[8], uint32_t (&hi)[8], u
 #pragma unroll
     for (int c = 0; c < 8; c++)
       if (MASK == 0 || (MASK == 1 && c < r) || (MASK == 2 && c >= r) || (MASK == 3 && 2 * r < c) ||
-          (MASK == 4 && 2 * r - c < 8))
+          (MASK == 4 && 2 * r - c < 8) || (MASK == 5 && r < 4))
         mac3(lo[c], hi[c], tp[c], a[r], w[OFF + 8 + c - r]);
 }
 
@@ -134,6 +135,7 @@ template <class X, class Y, class Sink>
 __device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, int cb_lo, int cb_hi, Sink &&sink) {
   const int Mx = (lx + 7) >> 3, My = (ly + 7) >> 3;
   const int Mo = min(Mx + My, cb_hi);
+  const bool half_rows = (lx & 7) != 0 && (lx & 7) <= 4;           // x's last block: rows 4..7 zero
   uint32_t c0 = 0u, c1 = 0u;
 #pragma unroll 1
   for (int cb = cb_lo; cb < Mo; cb++) {
@@ -163,8 +165,10 @@ __device__ __forceinline__ void tprod(const X &x, int lx, const Y &y, int ly, in
     int i = i0;
     if (cb >= My) step(i++, std::integral_constant<int, 1>{});   // upper window half in the guard
     const int iend = i1 == cb ? i1 : i1 + 1;                       // i = cb: lower half in the guard
+    const bool rows4 = half_rows && iend == Mx && i < iend;        // the loop ends on x's last block
 #pragma unroll 2
-    for (; i < iend; i++) step(i, std::integral_constant<int, 0>{});
+    for (; i < iend - (rows4 ? 1 : 0); i++) step(i, std::integral_constant<int, 0>{});
+    if (rows4) step(i++, std::integral_constant<int, 5>{});
     if (i1 == cb) tile_mac<2>(lo, hi, tp, a, w);
     uint32_t L[10];
     columns_to_limbs<8>(lo, hi, tp, L);
