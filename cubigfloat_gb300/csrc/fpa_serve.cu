@@ -169,6 +169,42 @@ class CopyPool {
 // share, deferred-list entry, three exponents, three mantissas)
 uint64_t op_bytes(uint32_t n) { return 32 + 4 + 16 + 4 + 12 + 12ull * n; }
 
+// The resident store's free blocks (offset -> bytes): first fit, and a released block merges
+// with free neighbours on both sides, so the free list never holds two adjacent blocks.
+struct ResidentStore {
+  std::map<uint64_t, uint64_t> free_blocks;
+  void reset(uint64_t cap) {
+    free_blocks.clear();
+    if (cap) free_blocks.emplace(0, cap);
+  }
+  // offset of a block of `bytes`, or UINT64_MAX when no free block is large enough
+  uint64_t alloc(uint64_t bytes) {
+    for (auto it = free_blocks.begin(); it != free_blocks.end(); ++it) {
+      if (it->second < bytes) continue;
+      const uint64_t off = it->first, rest = it->second - bytes;
+      free_blocks.erase(it);
+      if (rest) free_blocks.emplace(off + bytes, rest);
+      return off;
+    }
+    return UINT64_MAX;
+  }
+  void release(uint64_t off, uint64_t bytes) {
+    auto it = free_blocks.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != free_blocks.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_blocks.erase(nx);
+    }
+    if (it != free_blocks.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_blocks.erase(it);
+      }
+    }
+  }
+};
+
 struct Slot {
   cudaStream_t st = nullptr, side[2] = {nullptr, nullptr};
   cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr}, done = nullptr;
@@ -207,29 +243,10 @@ struct fpa_server_s {
   // statistics
   std::atomic<uint64_t> jobs_done{0}, ops_done{0}, batches{0}, peak_bytes{0}, resident{0}, failures{0};
   std::atomic<uint64_t> cost_ns[4] = {{0}, {0}, {0}, {0}};   // pack, h2d, device, d2h
-  // resident store: free blocks (offset -> bytes), guarded by mu
+  // resident store, its free blocks guarded by mu
   uint8_t *d_res = nullptr;
   uint64_t res_cap = 0;
-  std::map<uint64_t, uint64_t> res_free;
-  uint64_t res_alloc(uint64_t bytes) {
-    for (auto it = res_free.begin(); it != res_free.end(); ++it) {
-      if (it->second < bytes) continue;
-      const uint64_t off = it->first, rest = it->second - bytes;
-      res_free.erase(it);
-      if (rest) res_free.emplace(off + bytes, rest);
-      return off;
-    }
-    return UINT64_MAX;
-  }
-  void res_release(uint64_t off, uint64_t bytes) {
-    auto it = res_free.emplace(off, bytes).first;
-    auto nx = std::next(it);
-    if (nx != res_free.end() && it->first + it->second == nx->first) { it->second += nx->second; res_free.erase(nx); }
-    if (it != res_free.begin()) {
-      auto pv = std::prev(it);
-      if (pv->first + pv->second == it->first) { pv->second += it->second; res_free.erase(it); }
-    }
-  }
+  ResidentStore res_store;
 
   uint64_t now() const {
     return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(Clock::now() - t0).count();
@@ -568,7 +585,7 @@ extern "C" fpa_result fpa_server_create_resident(fpa_server_t *out, const fpa_se
   if (ok && resident_bytes) {
     srv->res_cap = align256(resident_bytes);
     ok = cudaMalloc(&srv->d_res, srv->res_cap) == cudaSuccess;
-    if (ok) srv->res_free.emplace(0, srv->res_cap);
+    if (ok) srv->res_store.reset(srv->res_cap);
   }
   if (!ok) { fpa_server_destroy(srv); return fpa_device_error; }
   const unsigned hw = std::thread::hardware_concurrency();
@@ -627,7 +644,7 @@ extern "C" int64_t fpa_server_submit_ex(fpa_server_t srv, uint32_t precision, ui
   }
   if (j->keep) {                                  // a block of the resident store: exponents, then limbs
     j->res_bytes = align256((size_t)count * 4) + align256((size_t)count * j->n * 4);
-    j->res_off = srv->res_cap ? srv->res_alloc(j->res_bytes) : UINT64_MAX;
+    j->res_off = srv->res_cap ? srv->res_store.alloc(j->res_bytes) : UINT64_MAX;
     if (j->res_off == UINT64_MAX) return -(int64_t)fpa_invalid_counts;       // the resident store is full
   }
   if (j->a_src) j->a_src->deps++;
@@ -673,7 +690,7 @@ extern "C" fpa_result fpa_server_release(fpa_server_t srv, int64_t job) {
   Job *j = it->second.get();
   if (j->state != JOB_DONE && j->state != JOB_FAILED) return fpa_math_error;
   if (j->deps > 0) return fpa_math_error;         // pending jobs still read its kept result
-  if (j->keep) srv->res_release(j->res_off, j->res_bytes);
+  if (j->keep) srv->res_store.release(j->res_off, j->res_bytes);
   srv->jobs.erase(it);
   return fpa_success;
 }
