@@ -22,14 +22,16 @@
 // far inside the 2^20-unit margin; the exact correction is unchanged.  A 4096-bit division
 // forms about 12K limb products this way, against 21.8K with whole products.
 //
-// Products (tprod) are column-block product scans with an 8x8 register tile (96-bit
-// column sums fed by mac3), the tile loop unrolled twice so that the next tile's operands
-// load while the current one multiplies, and no bounds checks: every buffer a product reads
-// sits in zero guard limbs, so the tiles may read past either end (an operand read as the
-// product's second factor needs 8 zero limbs below it and zeros up to 8 limbs past its
-// length rounded up to 8; the first factor only the zeros above).  The loads of the next
-// tile read up to 8 more limbs below a second factor and past a first factor (not used):
-// they lie inside the layouts below.
+// Products are column-block product scans with an 8x8 register tile (96-bit column sums
+// fed by mac3) and no bounds checks: tprod (one output block per pass, the tile loop
+// unrolled twice so that the next tile's operands load while the current one multiplies,
+// and tiles that would multiply zero guard limbs skip them), tprod2 (two output blocks per
+// pass, mul's) and tsqr (a square on its symmetric half).  Every buffer a product reads
+// sits in zero guard limbs, so the tiles may read past either end: an operand needs zeros
+// in the 8 limbs below it and from its length to 8 limbs past its length rounded up to 8,
+// and 8 more readable limbs beyond each of those (the next tile's loads and tprod2's wider
+// window read them without using them).  The layouts below provide that, and
+// tests/test_tile_products_host.py holds the three routines to it.
 //
 // Storage.  A thread's limb j of a buffer is at base[32*j] (the warp's 32 threads
 // interleaved limb by limb, so the 32 threads reading one limb index touch 32 consecutive
