@@ -224,8 +224,8 @@ def mpfr_leg(data, gpu_results, threads, count=MPFR_SAMPLE):
 # restricted to the limbs that are read, sqrt's square on its symmetric half.
 # tile_products() mirrors their 8x8-tile block ranges (tprod: output blocks [cb_lo, cb_hi)
 # of an lx x ly product, block cb spanning x blocks max(0, cb-My) .. min(cb, Mx-1); 64
-# products a tile, 36 for an edge tile whose window is half zero guard, 32 for a tile of x's
-# last block when it holds 1 to 4 limbs; tprod2, mul's: two
+# products a tile, 28 or 36 for an edge tile whose window is half zero guard, 32 for a tile of
+# x's last block when it holds 1 to 4 limbs; tprod2, mul's: two
 # blocks per pass; tsqr: the tiles below the diagonal), so that the roofline can also report
 # how busy the multiplier is on the products the first pass executes (deferred operations
 # excluded).
@@ -238,7 +238,8 @@ def _tprod(lx, ly, cb_lo, cb_hi):
     total = 0
     for cb in range(cb_lo, min(mx + my, cb_hi)):
         i0, i1 = max(0, cb - my), min(cb, mx - 1)
-        total += 64 * (i1 - i0 + 1) - (28 if cb >= my else 0) - (28 if i1 == cb else 0)
+        # a first tile in the guard keeps 28 products, a last tile 36
+        total += 64 * (i1 - i0 + 1) - (36 if cb >= my else 0) - (28 if i1 == cb else 0)
         iend, i = (i1 if i1 == cb else i1 + 1), i0 + (1 if cb >= my else 0)
         if half_rows and iend == mx and i < iend:      # x's last block, rows 4..7 zero
             total -= 32
@@ -277,12 +278,13 @@ def _tsqr(lx, cb_hi):
     total = 0
     for cb in range(0, min(2 * mx, cb_hi)):
         i0, d = max(0, cb - mx), cb // 2
-        total += 64 * (d - i0) - (28 if (cb >= mx and i0 < d) else 0) + (52 if cb & 1 else 20)
+        total += 64 * (d - i0) - (36 if (cb >= mx and i0 < d) else 0) + (52 if cb & 1 else 20)
     return total
 
 
 def tile_products(op, n):
-    """Limb products (64 per 8x8 tile) of the first pass of one operation at n limbs."""
+    """Limb products the first pass of one operation at n limbs executes in its tile products
+    (the one-thread register levels below them are not counted)."""
     blk = lambda keep: max(0, keep - 2) // 8
     big = 1 << 20
     if op == "mul":

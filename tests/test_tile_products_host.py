@@ -2,7 +2,9 @@
 one output block per pass with the zero half of edge tiles skipped; tprod2: two output blocks
 per pass, mul's; tsqr: a square on its symmetric half), compiled for the host from the
 device source and checked limb for limb against exact integer products, over a sweep of
-operand lengths and output block ranges.
+operand lengths and output block ranges.  The number of limb products each routine executes
+is counted too and compared with the model bench.py reports its executed-product roofline
+from.
 
 Operands are read through a checking view that holds each routine to the guard contract the
 kernels' layouts provide: zeros from limb len up to 8 limbs past len rounded up to 8 and
@@ -15,12 +17,14 @@ import subprocess
 import numpy as np
 import pytest
 
+import bench
 from test_thread_newton_host import host_body
 
 MAIN = r"""
 }  // namespace gfpa
 using namespace gfpa;
 static int g_bad = 0;
+extern long g_mac3;
 // a buffer of len limbs at stride TS with the guard zones of the kernels' layouts
 struct Buf {
   std::vector<uint32_t> mem;
@@ -60,10 +64,11 @@ int main() {
       for (int q = 0; q < 8; q++) out.push_back(o[q]);
     };
     g_bad = 0;
+    g_mac3 = 0;
     if (kind == 0) tprod(CV{&bx}, lx, CV{&by}, ly, cb_lo, cb_hi, sink);
     else if (kind == 1) tprod2(CV{&bx}, lx, CV{&by}, ly, cb_lo, cb_hi, sink);
     else tsqr(CV{&bx}, lx, cb_hi, sink);
-    printf("%d %d", g_bad, (int)out.size());
+    printf("%d %ld %d", g_bad, g_mac3, (int)out.size());
     for (uint32_t v : out) printf(" %u", v);
     printf("\n");
   }
@@ -79,10 +84,19 @@ def exe(tmp_path_factory):
         pytest.skip("g++ not found")
     d = tmp_path_factory.mktemp("tiles")
     src, out = d / "tiles.cpp", d / "tiles"
-    src.write_text(host_body() + MAIN)
+    src.write_text(counting(host_body()) + MAIN)
     r = subprocess.run([cxx, "-O1", "-std=c++17", "-o", str(out), str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
     return str(out)
+
+
+MAC3 = "static inline void mac3(uint32_t &lo, uint32_t &hi, uint32_t &tp, uint32_t a, uint32_t b) {"
+
+
+def counting(body):
+    """The host source with every mac3 call counted (g_mac3)."""
+    assert body.count(MAC3) == 1
+    return body.replace(MAC3, "}\nlong g_mac3 = 0;\nnamespace gfpa {\n" + MAC3 + "\n  g_mac3++;")
 
 
 def to_int(limbs):
@@ -146,10 +160,16 @@ def test_products_match_integers(exe, kind):
     cs = cases(100 + kind, 1500)
     lines = [f"{kind} {lx} {ly} {lo} {hi} " + " ".join(map(str, x + y)) for lx, ly, lo, hi, x, y in cs]
     for (lx, ly, lo, hi, x, y), row in zip(cs, run(exe, lines)):
-        bad, n, got = row[0], row[1], row[2:]
+        bad, macs, n, got = row[0], row[1], row[2], row[3:]
         assert bad == 0, ("read outside the guard zones or block order", kind, lx, ly, lo, hi)
         assert got == expected(x, y, lo, hi), (kind, lx, ly, lo, hi)
         assert n == len(got)
+        # limb products executed = the bench's model (tprod2 adds 2 carry steps per block pair)
+        mo = min((lx + 7) // 8 + (ly + 7) // 8, hi)
+        if kind == 0:
+            assert macs == bench._tprod(lx, ly, lo, hi), (lx, ly, lo, hi)
+        else:
+            assert macs == bench._tprod2(lx, ly, lo, hi) + 2 * (max(0, mo - lo) // 2), (lx, ly, lo, hi)
 
 
 def test_square_matches_integers(exe):
@@ -164,9 +184,11 @@ def test_square_matches_integers(exe):
                 cs.append((lx, cb_hi, limbs(rng, lx, pat)))
     lines = [f"2 {lx} 0 0 {hi} " + " ".join(map(str, x)) for lx, hi, x in cs]
     for (lx, hi, x), row in zip(cs, run(exe, lines)):
-        bad, got = row[0], row[2:]
+        bad, macs, got = row[0], row[1], row[3:]
         assert bad == 0, ("read outside the guard zones or block order", lx, hi)
         assert got == expected(x, x, 0, hi), (lx, hi)
+        # the bench's model plus 2 carry steps per block
+        assert macs == bench._tsqr(lx, hi) + 2 * min(2 * ((lx + 7) // 8), hi), (lx, hi)
 
 
 def test_two_block_product_equals_one_block(exe):
@@ -174,4 +196,5 @@ def test_two_block_product_equals_one_block(exe):
     cs = cases(5, 600)
     l0 = [f"0 {lx} {ly} {lo} {hi} " + " ".join(map(str, x + y)) for lx, ly, lo, hi, x, y in cs]
     l1 = [f"1 {lx} {ly} {lo} {hi} " + " ".join(map(str, x + y)) for lx, ly, lo, hi, x, y in cs]
-    assert run(exe, l0) == run(exe, l1)
+    r0, r1 = run(exe, l0), run(exe, l1)
+    assert [[r[0]] + r[2:] for r in r0] == [[r[0]] + r[2:] for r in r1]
